@@ -1,0 +1,285 @@
+/* vrestir.h -- C ABI of the GB300-native Volumetric ReSTIR frame loop (libvrestir.so).
+ *
+ * This library replaces the per-frame path of the `VolumetricReSTIR` render pass of
+ * DQLin/VolumetricReSTIRRelease.  Each entry point names the reference interface it stands
+ * in for (paths relative to the reference repository):
+ *
+ *   plugin discovery / create  Source/RenderPasses/VolumetricReSTIR/VolumetricReSTIR.cpp:61-70
+ *                              (getPasses -> VolumetricReSTIR::create(RenderContext*, Dictionary))
+ *   options                    VolumetricReSTIR.h:130-207 (VolumetricReSTIRParams),
+ *                              VolumetricReSTIR.cpp:1280-1347 (setDictionary / option changes)
+ *   scene binding              VolumetricReSTIR.cpp:1218-1256 (setScene), Falcor Scene.cpp:2754
+ *                              (Scene::addGVDBVolume), EnvMapSampler.cpp:39-100 (importance map)
+ *   per-frame call             Source/Falcor/RenderGraph/RenderPass.h:114 (execute), implemented by
+ *                              VolumetricReSTIR.cpp:303-906; output channel `accumulated_color`
+ *   reservoir layout           HostDeviceSharedDefinitions.h:16-71 (Reservoir, ExtraBounceReservoir,
+ *                              ReservoirFeatures)
+ *
+ * Conventions: every function returns an int status (VR_OK = 0) unless stated otherwise;
+ * exceptions never cross this boundary.  A context owns all of its device buffers; output
+ * pointers are owned by the caller.  A context is not thread-safe; separate contexts may be
+ * used from separate threads.  All GPU work of a call is issued on the caller's stream
+ * (a cudaStream_t passed as void*; NULL = legacy default stream).
+ */
+#ifndef VRESTIR_H
+#define VRESTIR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (reference: exceptions / logError, VolumetricReSTIR.cpp:196) ---- */
+#define VR_OK 0
+#define VR_ERR_INVALID_ARG 1
+#define VR_ERR_OOM 2
+#define VR_ERR_CUDA 3
+#define VR_ERR_LOOP_LIMIT 4     /* a bounded device loop hit its limit (status word set) */
+#define VR_ERR_UNSUPPORTED 5    /* option value outside the supported surface */
+#define VR_ERR_STATE 6          /* call order: e.g. render before a volume is bound */
+
+/* ---- enums, values as in HostDeviceSharedConstants.slang:5-16, 29-31 ---- */
+#define VR_MIS_NONE 0
+#define VR_MIS_TALBOT 1
+#define VR_SAMPLER_HAMMERSLEY 0
+#define VR_SAMPLER_R2 1
+#define VR_TRACK_RATIO 0
+#define VR_TRACK_ANALYTIC 1
+#define VR_TRACK_RAY_MARCHING 2
+#define VR_TRACK_RESIDUAL_RATIO 3
+#define VR_TRACK_ANALOG_RESIDUAL_RATIO 4
+#define VR_REPROJ_LINEAR 0
+#define VR_REPROJ_NONE 1
+#define VR_REPROJ_NO_BACKGROUND 2
+
+#define VR_NUM_MAX_MIPS 8           /* kNumMaxMips; slots 0-7 normal, 8-15 conservative */
+#define VR_NUM_SLOTS 16
+#define VR_MAX_BOUNCES 4            /* max path length supported by this build */
+#define VR_BRICK 8                  /* brick edge in voxels */
+#define VR_BRICK_APRON 10           /* stored brick edge: 8 + 2 x apron of 1 */
+
+/* Options: same names, meanings and defaults as VolumetricReSTIRParams
+ * (VolumetricReSTIR.h:130-207).  Members absent here (surface scenes, vertex reuse, mesh
+ * lights, animation) are outside this path.  vr_options_default() fills the defaults. */
+typedef struct vr_options {
+    int32_t mMaxBounces;                        /* 1 */
+    int32_t mEnableTemporalReuse;               /* 1 */
+    int32_t mEnableSpatialReuse;                /* 1 */
+    int32_t mUseReference;                      /* 0: volume path tracer instead of ReSTIR */
+    int32_t mUseEnvironmentLights;              /* 1 */
+    int32_t mUseAnalyticLights;                 /* 0 */
+    int32_t mBaselineSamplePerPixel;            /* 1 */
+    int32_t mVisualizeTotalTransmittance;       /* 0 */
+    int32_t mInitialBaseMipLevel;               /* 1 */
+    int32_t mInitialM;                          /* 4 */
+    int32_t mInitialLightSamples;               /* 1 */
+    int32_t mInitialLightingMipLevel;           /* 2 */
+    int32_t mInitialVisibilityUseLinearSampler; /* 0 */
+    int32_t mInitialLightingUseLinearSampler;   /* 1 */
+    uint32_t mInitialLightingTrackingMethod;    /* VR_TRACK_RAY_MARCHING */
+    float mInitialVisibilityTStepScale;         /* 1 */
+    float mInitialLightingTStepScale;           /* 2 */
+    int32_t mInitialUseRussianRoulette;         /* 1 */
+    int32_t mInitialUseCoarserGridForIndirectBounce; /* 1 */
+    float mTemporalReuseMThreshold;             /* 4 */
+    uint32_t mTemporalReprojectionMode;         /* VR_REPROJ_LINEAR */
+    uint32_t mTemporalMISMethod;                /* VR_MIS_TALBOT */
+    int32_t mTemporalReprojectionMipLevel;      /* 1 */
+    int32_t mSpatialReuseRounds;                /* 1 */
+    int32_t mSpatialVisibilityMipLevel;         /* 1 */
+    int32_t mSpatialLightingMipLevel;           /* 1 */
+    int32_t mSpatialVisibilityUseLinearSampler; /* 1 */
+    int32_t mSpatialLightingUseLinearSampler;   /* 1 */
+    float mSpatialVisibilityTStepScale;         /* 1 */
+    float mSpatialLightingTStepScale;           /* 1 */
+    uint32_t mSpatialVisibilityTrackingMethod;  /* VR_TRACK_RAY_MARCHING */
+    uint32_t mSpatialLightingTrackingMethod;    /* VR_TRACK_RAY_MARCHING */
+    uint32_t mRandomSamplerType;                /* VR_SAMPLER_R2 */
+    float mSampleRadius;                        /* 10 */
+    int32_t mSpatialSampleCount;                /* 4 (includes the centre pixel) */
+    uint32_t mSpatialMISMethod;                 /* VR_MIS_TALBOT */
+    int32_t mFinalLightSamples;                 /* 1 */
+    int32_t mFinalVisibilitySamples;            /* 1 */
+    uint32_t mFinalVisibilityTrackingMethod;    /* VR_TRACK_ANALYTIC */
+    uint32_t mFinalLightTrackingMethod;         /* VR_TRACK_ANALYTIC */
+    float mFinalTStepScale;                     /* 0.2 */
+} vr_options;
+
+/* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */
+typedef struct vr_medium {
+    float sigma_a[3];
+    float sigma_s[3];             /* sigma_t = sigma_a.x + sigma_s.x (grey) */
+    float g;                      /* Henyey-Greenstein anisotropy */
+    float density_scale;          /* densityScaleFactorByScaling = DensityScale / worldScaling */
+} vr_medium;
+
+/* Procedural sparse volume (density in [0,1], fBm Perlin noise): the synthetic stand-in for the
+ * reference's .vbx assets.  kind: 0 = fBm x smooth sphere mask (dense), 1 = thresholded fBm
+ * (sparse).  The volume occupies the world box [world_min, world_min + res*voxel_size). */
+typedef struct vr_procedural_desc {
+    int32_t kind;
+    int32_t res;                  /* voxels per axis at mip 0 (multiple of 8 * 2^(num_mips-1)) */
+    int32_t num_mips;             /* 1..VR_NUM_MAX_MIPS; normal + conservative pyramids */
+    int32_t octaves;
+    uint32_t seed;
+    float lacunarity, gain;
+    float base_frequency;         /* noise frequency across the unit cube */
+    float mask_radius;            /* kind 0: sphere radius in the unit cube */
+    float threshold;              /* kind 1: density = clamp((n - thr)/(1 - thr)) */
+    float world_min[3];
+    float voxel_size;             /* world size of one mip-0 voxel */
+    int32_t fp16;                 /* store bricks as FP16 (precision form) */
+} vr_procedural_desc;
+
+typedef struct vr_volume vr_volume;   /* opaque host-side sparse brick grid, all mip slots */
+
+/* Raw view of one mip slot (what the GPU reads and what the oracle consumes). */
+typedef struct vr_grid_view {
+    int32_t valid;
+    int32_t res[3];
+    float bmin[3], bmax[3];       /* index-space bounds [0, res) */
+    float world_to_index[16];     /* row-vector convention: idx = (p, 1) * M */
+    float max_value;              /* max voxel value of this slot */
+    int32_t num_l1;
+    int32_t num_bricks;
+    const int32_t* root_child;    /* 32^3: level-2 child list -> level-1 node, -1 = empty */
+    const int32_t* l1_vmin;       /* 4 ints per level-1 node (x, y, z, 0) */
+    const int32_t* l1_child;      /* 16^3 per level-1 node -> brick id, -1 = empty */
+    const int32_t* brick_vmin;    /* 4 ints per brick */
+    const float* brick_bounds;    /* 4 floats per brick: min, max, avg(sum/512), 0 */
+    const float* brick_f32;       /* 10^3 floats per brick (apron 1), or NULL */
+    const uint16_t* brick_f16;    /* 10^3 halves per brick, or NULL */
+} vr_grid_view;
+
+typedef struct vr_volume_info {
+    int32_t num_mips;
+    int32_t res;
+    float voxel_size;             /* world size of a mip-0 voxel: tStep * worldScaling */
+    float supervoxel_diag;        /* superVoxelWorldSpaceDiagonalLength (Scene.cpp:3076-3080) */
+    int32_t num_bricks[VR_NUM_SLOTS];
+    int64_t device_bytes;         /* bytes the grid occupies once bound to a context */
+    int32_t fp16;
+} vr_volume_info;
+
+typedef struct vr_point_light {   /* LightHelpers.slang:223-242 (point light, uniform emission) */
+    float pos[3];
+    float intensity[3];
+} vr_point_light;
+
+/* Lat-long environment map (EnvMap.slang:45-50) with a linear (wrap u / clamp v) lookup. */
+typedef struct vr_env_map {
+    const float* rgb;             /* width * height * 3 floats, row-major, host memory */
+    int32_t width, height;
+    float scale[3];               /* intensity * tint */
+    float rotation[9];            /* local->world, row-vector convention (EnvMapData.transform) */
+} vr_env_map;
+
+typedef struct vr_camera {        /* Camera.cpp:183-189 pinhole frame, no jitter */
+    float pos[3];
+    float target[3];
+    float up[3];
+    float fov_y;                  /* radians */
+    float near_z, far_z;
+} vr_camera;
+
+/* AoS reservoir record exactly as HostDeviceSharedDefinitions.h:16-45 lays it out
+ * (32 bytes for max path length 1; 36 bytes with extraBounceStartId otherwise). */
+typedef struct vr_reservoir_aos {
+    float runningSum;
+    float M;
+    float depth;
+    float p_y;
+    float lightUV[2];
+    int32_t lightID;
+    int32_t sampledPixel;
+    int32_t extraBounceStartId;   /* present in the exported stream only if mMaxBounces > 1 */
+} vr_reservoir_aos;
+
+typedef struct vr_context vr_context;
+
+/* ---- options ---- */
+void vr_options_default(vr_options* o);                        /* VolumetricReSTIR.h:130-207 */
+
+/* ---- volumes (Scene::addGVDBVolume, Scene.cpp:2754-3279; mips and conservative mips as in
+ *      gvdb_volume_gvdb.cpp:2700-2862; brick bounds as in Scene.cpp:2983-3012) ---- */
+int vr_volume_create_procedural(const vr_procedural_desc* d, vr_volume** out);
+int vr_volume_create_dense(const float* density, int32_t res, int32_t num_mips,
+                           const float world_min[3], float voxel_size, int32_t fp16,
+                           vr_volume** out);
+void vr_volume_destroy(vr_volume* v);
+int vr_volume_get_info(const vr_volume* v, vr_volume_info* info);
+int vr_volume_get_slot(const vr_volume* v, int32_t slot, vr_grid_view* view);
+
+/* ---- context lifecycle (getPasses/create, VolumetricReSTIR.cpp:61-70) ---- */
+vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int32_t* err);
+void vr_destroy(vr_context* ctx);
+const char* vr_last_error(const vr_context* ctx);
+/* Any change resets the history like mOptionsChanged (VolumetricReSTIR.cpp:349-359). */
+int vr_set_options(vr_context* ctx, const vr_options* opts);
+int vr_get_options(const vr_context* ctx, vr_options* opts);
+int vr_resize(vr_context* ctx, int32_t width, int32_t height);
+
+/* ---- scene binding (setScene, VolumetricReSTIR.cpp:1218-1256) ---- */
+int vr_set_volume(vr_context* ctx, const vr_volume* vol, const vr_medium* medium);
+int vr_set_lights(vr_context* ctx, const vr_point_light* lights, int32_t num_lights,
+                  const vr_env_map* env);
+
+/* ---- per-frame call (execute, VolumetricReSTIR.cpp:303-906) ----
+ * out_rgba_device: width*height float4 (RGBA32F, `accumulated_color`), device memory.
+ * out_mvec_device: optional width*height float2 motion vectors (mOutputMotionVec), or NULL. */
+int vr_render_frame(vr_context* ctx, const vr_camera* cam, float* out_rgba_device,
+                    float* out_mvec_device, void* stream);
+/* Same frame, host output buffer: copies the image back (synchronises the stream). */
+int vr_render_frame_host(vr_context* ctx, const vr_camera* cam, float* out_rgba_host,
+                         void* stream);
+
+/* ---- FP64 converged reference (IntegrateByVolumePathTracing,
+ *      VolumePathTracingFunctions.slang:3-131, accumulated like AccumulatePass'
+ *      accumulateDouble, Accumulate.cs.slang:100).  Renders num_frames frames of
+ *      mBaselineSamplePerPixel paths each, adding each frame's RGB into accum_device
+ *      (width*height*3 doubles, device memory, caller-owned and caller-zeroed). ---- */
+int vr_render_reference(vr_context* ctx, const vr_camera* cam, int32_t first_frame,
+                        int32_t num_frames, double* accum_device, void* stream);
+
+/* ---- state export / import (checkpoint of the history; no hidden sync elsewhere) ----
+ * which: 0 = current reservoirs (output of the last frame), 1 = temporal history.
+ * host_aos receives width*height records of vr_reservoir_bytes(ctx) bytes. */
+int32_t vr_reservoir_bytes(const vr_context* ctx);
+int vr_export_reservoirs(vr_context* ctx, int32_t which, void* host_aos, size_t bytes);
+/* extra-bounce records (float3 wi_dist, HostDeviceSharedDefinitions.h:49-52),
+ * width*height*(mMaxBounces-1)*3 floats. */
+int vr_export_extra_bounces(vr_context* ctx, int32_t which, float* host, size_t bytes);
+/* features (int noReflectiveSurface, float transmittance), width*height records. */
+int vr_export_features(vr_context* ctx, void* host, size_t bytes);
+/* Full state blob (all history buffers, frame counter, previous camera). */
+int64_t vr_state_bytes(const vr_context* ctx);
+int vr_export_state(vr_context* ctx, void* host, size_t bytes);
+int vr_import_state(vr_context* ctx, const void* host, size_t bytes);
+int32_t vr_frame_count(const vr_context* ctx);
+
+/* ---- instrumentation ---- */
+/* Per-kernel device time of the last vr_render_frame (milliseconds), CUDA events. */
+int vr_last_timings(const vr_context* ctx, float* ms, int32_t max_entries, int32_t* n);
+/* Device time per kernel stage (0: k_initial, 1: spatial/final stage) summed over the frames
+ * rendered since the last reset, from CUDA events recorded on the caller's stream.  Waits for
+ * those events; call it outside a timed region. */
+int vr_kernel_time_totals(vr_context* ctx, float* ms, int32_t max_entries, int32_t* frames, int32_t reset);
+/* Kernel launches issued by the last vr_render_frame. */
+int32_t vr_last_launch_count(const vr_context* ctx);
+/* Host->device and device->host bytes moved by the last frame call (scene constants and
+ * launch parameters in; the image out for vr_render_frame_host). */
+int vr_last_transfer_bytes(const vr_context* ctx, int64_t* h2d, int64_t* d2h);
+
+/* ---- self tests: elementary functions and the RNG evaluated by a device kernel, so callers
+ *      can check device/host bit equality.  op: 0 exp, 1 log, 2 sin, 3 cos, 4 atan2, 5 acos,
+ *      6 pow, 7 sqrt.  In/out are host arrays of n floats. ---- */
+int vr_selftest_math(int32_t op, const float* a, const float* b, float* out, int32_t n);
+/* For n pixel cases (px, py, sampleNumber) returns the first `draws` values of sampleNext1D. */
+int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VRESTIR_H */

@@ -1,0 +1,165 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, and only
+as the checker; the product path never calls it.
+"""
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+from . import build as _build
+
+HERE = pathlib.Path(__file__).resolve().parent
+
+
+def _load():
+    lib = C.CDLL(str(_build.build()))
+    P = C.c_void_p
+    sig = {
+        "vro_create": (P, [P, C.c_int, C.c_int]),
+        "vro_destroy": (None, [P]),
+        "vro_set_threads": (None, [P, C.c_int]),
+        "vro_set_options": (None, [P, P]),
+        "vro_set_volume": (C.c_int, [P, P, C.c_int, P, C.c_float, C.c_float, C.c_int]),
+        "vro_set_lights": (C.c_int, [P, P, C.c_int, P]),
+        "vro_render_frame": (C.c_int, [P, P, P, P]),
+        "vro_frame_count": (C.c_int, [P]),
+        "vro_voxel_reads": (None, [P]),
+        "vro_export_reservoirs": (C.c_int, [P, C.c_int, P]),
+        "vro_export_extra": (C.c_int, [P, C.c_int, P]),
+        "vro_export_features": (C.c_int, [P, P]),
+        "vro_env_importance": (C.c_int, [P, C.c_int, P]),
+        "vro_render_reference": (C.c_int, [P, P, C.c_int, C.c_int, P]),
+        "vro_transmittance": (C.c_float, [P, P, P, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint32]),
+        "vro_sample_distance": (None, [P, P, P, C.c_int, C.c_int, C.c_uint32, P]),
+        "vro_density_world": (C.c_float, [P, P, C.c_int]),
+        "vro_math": (C.c_int, [C.c_int, P, P, P, C.c_int]),
+        "vro_rng": (None, [P, C.c_int, C.c_int, P]),
+        "vro_xoshiro": (None, [P, C.c_int, P]),
+        "vro_splitmix": (None, [C.c_uint64, C.c_int, P]),
+    }
+    for k, (r, a) in sig.items():
+        f = getattr(lib, k)
+        f.restype = r
+        f.argtypes = a
+    return lib
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = _load()
+    return _LIB
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """CPU restatement of the pass, driven through the same data as the GPU library."""
+
+    def __init__(self, width, height, options, threads=0):
+        self.L = lib()
+        self.width, self.height = width, height
+        self._opts = options
+        self._h = self.L.vro_create(C.byref(options), width, height)
+        if threads:
+            self.L.vro_set_threads(self._h, threads)
+        self.max_bounces = options.mMaxBounces
+
+    def set_options(self, options):
+        self._opts = options
+        self.max_bounces = options.mMaxBounces
+        self.L.vro_set_options(self._h, C.byref(options))
+
+    def set_volume(self, volume, medium):
+        views = volume.views()
+        info = volume.info()
+        self._volume = volume
+        self.L.vro_set_volume(self._h, C.cast(views, C.c_void_p), 16, C.byref(medium), info.voxel_size,
+                              info.supervoxel_diag, info.num_mips)
+
+    def set_lights(self, lights, env_rgb=None, env_scale=(1.0, 1.0, 1.0)):
+        from volumetricrestirrelease_gb300 import capi
+        from volumetricrestirrelease_gb300.restir import env_struct
+        arr = (capi.PointLight * max(1, len(lights)))(*lights) if lights else None
+        env = None
+        if env_rgb is not None:
+            env, self._env_keep = env_struct(env_rgb, env_scale)
+        self.L.vro_set_lights(self._h, C.cast(arr, C.c_void_p) if arr else None, len(lights),
+                              C.byref(env) if env is not None else None)
+
+    def render_frame(self, camera, mvec=False):
+        out = np.zeros((self.height, self.width, 4), np.float32)
+        mv = np.zeros((self.height, self.width, 2), np.float32) if mvec else None
+        r = self.L.vro_render_frame(self._h, C.byref(camera), _ptr(out), _ptr(mv) if mv is not None else None)
+        if r != 0:
+            raise RuntimeError(f"oracle frame status {r}")
+        return (out, mv) if mvec else out
+
+    def render_reference(self, camera, first_frame, num_frames, accum=None):
+        if accum is None:
+            accum = np.zeros((self.height, self.width, 3), np.float64)
+        r = self.L.vro_render_reference(self._h, C.byref(camera), first_frame, num_frames, _ptr(accum))
+        if r != 0:
+            raise RuntimeError(f"oracle reference status {r}")
+        return accum
+
+    def export_reservoirs(self, which=0):
+        from volumetricrestirrelease_gb300.restir import RESERVOIR_DTYPE_36
+        out = np.zeros(self.width * self.height, RESERVOIR_DTYPE_36)
+        self.L.vro_export_reservoirs(self._h, which, _ptr(out))
+        return out
+
+    def export_extra(self, which=0):
+        n = self.width * self.height * max(self.max_bounces - 1, 1) * 3
+        out = np.zeros(n, np.float32)
+        self.L.vro_export_extra(self._h, which, _ptr(out))
+        return out[: self.width * self.height * max(self.max_bounces - 1, 0) * 3]
+
+    def export_features(self):
+        out = np.zeros(self.width * self.height * 2, np.int32)
+        self.L.vro_export_features(self._h, _ptr(out))
+        return out
+
+    def env_importance(self, mip):
+        d = 512 >> mip
+        out = np.zeros(d * d, np.float32)
+        self.L.vro_env_importance(self._h, mip, _ptr(out))
+        return out
+
+    @property
+    def frame_count(self):
+        return self.L.vro_frame_count(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self.L.vro_destroy(self._h)
+            self._h = None
+
+
+def voxel_reads():
+    """Voxel reads per pass since the last call: features, initial, temporal, spatial, final, reference."""
+    out = np.zeros(8, np.uint64)
+    lib().vro_voxel_reads(_ptr(out))
+    return out
+
+
+def math_op(op, a, b=None):
+    a = np.ascontiguousarray(a, np.float32)
+    out = np.zeros_like(a)
+    bb = np.ascontiguousarray(b, np.float32) if b is not None else None
+    lib().vro_math(op, _ptr(a), _ptr(bb) if bb is not None else None, _ptr(out), a.size)
+    return out
+
+
+def rng(cases, draws):
+    cases = np.ascontiguousarray(cases, np.uint32)
+    out = np.zeros((len(cases), draws), np.float32)
+    lib().vro_rng(_ptr(cases), len(cases), draws, _ptr(out))
+    return out

@@ -1,0 +1,1035 @@
+// context.cu -- host side of libvrestir: the C ABI, the per-frame orchestration
+// (VolumetricReSTIR::execute, VolumetricReSTIR.cpp:303-906) and the kernel instantiations.
+//
+// The context owns every device buffer: the sparse brick grid of each mip slot, the
+// environment map with its importance pyramid, and the SoA reservoir buffers (current,
+// spatial ping-pong, temporal history), the extra-bounce planes and the feature buffers.
+// All work of a call goes on the caller's stream; nothing synchronises except the
+// *_host variants, the exports and the status query.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/vrestir.h"
+#include "vr_kernels.cuh"
+#include "vr_volume.h"
+
+// per-path-length kernel objects (frame_kernels.cu compiled with VR_MB = 1..4)
+namespace vrk {
+#define VR_DECL(MB)                                                                                           \
+    cudaError_t upload_scene_##MB(const vrd::DevScene&, cudaStream_t);                                         \
+    void launch_initial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, dim3, dim3, cudaStream_t);     \
+    void launch_spatial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::SpatialParams&, dim3, dim3, cudaStream_t); \
+    void launch_final_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, int, dim3, dim3, cudaStream_t);  \
+    void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);
+VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
+#undef VR_DECL
+}
+
+using vr::f3;
+using vr::mk3;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------------------
+struct CamFrame {
+    f3 pos, U, V, W;
+    float view[16], proj[16];
+};
+
+// Camera.cpp:183-189 (pinhole frame, focal distance 1) and the glm lookAt / perspective
+// matrices the temporal pass reprojects with (depth range [0, 1]).
+CamFrame camera_frame(const vr_camera& c, int W, int H) {
+    CamFrame f;
+    f3 pos = mk3(c.pos[0], c.pos[1], c.pos[2]);
+    f3 tgt = mk3(c.target[0], c.target[1], c.target[2]);
+    f3 up = mk3(c.up[0], c.up[1], c.up[2]);
+    float aspect = (float)W / (float)H;
+    float th = vr::tan_(c.fov_y * 0.5f);
+    f.pos = pos;
+    f.W = vr::normalize(tgt - pos) * 1.f;
+    f.U = vr::normalize(vr::cross(f.W, up));
+    f.V = vr::normalize(vr::cross(f.U, f.W));
+    f.U = f.U * (1.f * th * aspect);
+    f.V = f.V * (1.f * th);
+    f3 fw = vr::normalize(tgt - pos);
+    f3 s = vr::normalize(vr::cross(fw, up));
+    f3 u = vr::cross(s, fw);
+    float* v = f.view;
+    for (int i = 0; i < 16; ++i) v[i] = 0.f;
+    v[0] = s.x; v[4] = s.y; v[8] = s.z;
+    v[1] = u.x; v[5] = u.y; v[9] = u.z;
+    v[2] = -fw.x; v[6] = -fw.y; v[10] = -fw.z;
+    v[12] = -vr::dot(s, pos); v[13] = -vr::dot(u, pos); v[14] = vr::dot(fw, pos); v[15] = 1.f;
+    float* p = f.proj;
+    for (int i = 0; i < 16; ++i) p[i] = 0.f;
+    p[0] = 1.f / (aspect * th);
+    p[5] = 1.f / th;
+    p[10] = c.far_z / (c.near_z - c.far_z);
+    p[11] = -1.f;
+    p[14] = -(c.far_z * c.near_z) / (c.far_z - c.near_z);
+    return f;
+}
+
+// SpatialReuse.cs.slang:64-81: the neighbour offsets of a round are the same for every pixel
+void neighbor_offsets(const vr_options& o, int r2TimeSeed, int offs[][2]) {
+    for (int sid = 0; sid < o.mSpatialSampleCount; ++sid) {
+        float ux, uy;
+        if (o.mRandomSamplerType == VR_SAMPLER_HAMMERSLEY) {
+            ux = (float)sid / (float)o.mSpatialSampleCount;
+            uint32_t i = (uint32_t)sid;
+            i = (i & 0x55555555u) << 1 | (i & 0xAAAAAAAAu) >> 1;
+            i = (i & 0x33333333u) << 2 | (i & 0xCCCCCCCCu) >> 2;
+            i = (i & 0x0F0F0F0Fu) << 4 | (i & 0xF0F0F0F0u) >> 4;
+            i = (i & 0x00FF00FFu) << 8 | (i & 0xFF00FF00u) >> 8;
+            i = (i << 16) | (i >> 16);
+            uy = (float)i * 2.3283064365386963e-10f;
+        } else if (sid == 0) {
+            ux = 0.f; uy = 0.f;
+        } else {
+            double m = (double)(r2TimeSeed * o.mSpatialSampleCount + sid);
+            double a = 0.754877669 * m, b = 0.569840296 * m;
+            ux = (float)(a - std::floor(a));
+            uy = (float)(b - std::floor(b));
+        }
+        float r = vr::sqrt_(ux), phi = vrd::kM_2PI * uy;
+        offs[sid][0] = vr::f2i(o.mSampleRadius * (r * vr::cos_(phi)));
+        offs[sid][1] = vr::f2i(o.mSampleRadius * (r * vr::sin_(phi)));
+    }
+}
+
+// lat-long env lookup, octahedral map and importance pyramid (EnvMapSamplerSetup.cs.slang)
+struct HostEnv {
+    std::vector<float> rgb;
+    int w = 0, h = 0;
+    std::vector<float> imp;    // concatenated mips
+    int off[12] = {};
+};
+float host_lerp(float a, float b, float t) { return a + (b - a) * t; }
+float signf_h(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
+void env_tex(const HostEnv& e, float u, float v, float c[3]) {
+    float x = u * (float)e.w - 0.5f, y = v * (float)e.h - 0.5f;
+    float fx0 = vr::floor_(x), fy0 = vr::floor_(y);
+    float fx = x - fx0, fy = y - fy0;
+    int ix = vr::f2i(fx0), iy = vr::f2i(fy0);
+    int x0 = ix % e.w; if (x0 < 0) x0 += e.w;
+    int x1 = (ix + 1) % e.w; if (x1 < 0) x1 += e.w;
+    int y0 = iy < 0 ? 0 : (iy >= e.h ? e.h - 1 : iy);
+    int y1 = iy + 1 < 0 ? 0 : (iy + 1 >= e.h ? e.h - 1 : iy + 1);
+    for (int k = 0; k < 3; ++k) {
+        float a = e.rgb[((size_t)y0 * e.w + x0) * 3 + k], b = e.rgb[((size_t)y0 * e.w + x1) * 3 + k];
+        float cc = e.rgb[((size_t)y1 * e.w + x0) * 3 + k], d = e.rgb[((size_t)y1 * e.w + x1) * 3 + k];
+        c[k] = host_lerp(host_lerp(a, b, fx), host_lerp(cc, d, fx), fy);
+    }
+}
+void build_importance(HostEnv& e) {
+    const int dim = 512, sx = 8, sy = 8, base = 9;
+    size_t total = 0;
+    for (int m = 0; m <= base; ++m) { e.off[m] = (int)total; total += (size_t)(dim >> m) * (dim >> m); }
+    e.imp.assign(total, 0.f);
+    const float invSamples = 1.f / (float)(sx * sy);
+    const float dimS = (float)(dim * sx);
+    int nt = std::max(1u, std::thread::hardware_concurrency());
+    std::atomic<int> next(0);
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+        th.emplace_back([&]() {
+            for (int py; (py = next.fetch_add(1)) < dim;)
+                for (int px = 0; px < dim; ++px) {
+                    float L = 0.f;
+                    for (int y = 0; y < sy; ++y)
+                        for (int x = 0; x < sx; ++x) {
+                            float ppx = ((float)(px * sx + x) + 0.5f) / dimS, ppy = ((float)(py * sy + y) + 0.5f) / dimS;
+                            // oct_to_ndir_equal_area_unorm (MathHelpers.slang:200-219)
+                            float qx = ppx * 2.f - 1.f, qy = ppy * 2.f - 1.f;
+                            float d = 1.f - (vr::fabs_(qx) + vr::fabs_(qy));
+                            float r = 1.f - vr::fabs_(d);
+                            float phi = (r > 0.f) ? ((vr::fabs_(qy) - vr::fabs_(qx)) / r + 1.f) * vrd::kM_PI_4 : 0.f;
+                            float f = r * vr::sqrt_(2.f - r * r);
+                            f3 dir = mk3(f * signf_h(qx) * vr::cos_(phi), f * signf_h(qy) * vr::sin_(phi), signf_h(d) * (1.f - r * r));
+                            // world_to_latlong_map (MathHelpers.slang:92-99)
+                            f3 pn = vr::normalize(dir);
+                            float u = vr::atan2_(pn.x, -pn.z) * vrd::kM_1_2PI + 0.5f;
+                            float v = vr::acos_(pn.y) * vrd::kM_1_PI;
+                            float c[3];
+                            env_tex(e, u, v, c);
+                            L += vr::luminance(mk3(c[0], c[1], c[2]));
+                        }
+                    e.imp[(size_t)py * dim + px] = L * invSamples;
+                }
+        });
+    for (auto& t : th) t.join();
+    for (int m = 1; m <= base; ++m) {
+        int d = dim >> m, ds = dim >> (m - 1);
+        const float* s = &e.imp[e.off[m - 1]];
+        float* o = &e.imp[e.off[m]];
+        for (int y = 0; y < d; ++y)
+            for (int x = 0; x < d; ++x) {
+                float a = s[(size_t)(2 * y) * ds + 2 * x], b = s[(size_t)(2 * y) * ds + 2 * x + 1];
+                float c = s[(size_t)(2 * y + 1) * ds + 2 * x], dd = s[(size_t)(2 * y + 1) * ds + 2 * x + 1];
+                o[(size_t)y * d + x] = (((a + b) + c) + dd) * 0.25f;
+            }
+    }
+}
+
+template <class T>
+T* dalloc(size_t n) {
+    T* p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+    return p;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------
+struct vr_context {
+    vr_options opts;
+    int W = 0, H = 0;
+    std::string err;
+    // scene
+    vrd::DevScene scene{};
+    std::vector<void*> sceneAllocs;
+    bool hasVolume = false;
+    int numMips = 0;
+    std::vector<void*> envAllocs;
+    HostEnv env;
+    // buffers
+    vrd::ResBuf res[3]{};      // 0 = perPixel[0], 1 = perPixel[1], 2 = temporal history
+    float* feat[2] = {nullptr, nullptr};
+    int featCurIdx = 0;
+    float* color = nullptr;
+    int allocMB = 0, allocW = 0, allocH = 0;
+    // frame state
+    int frameCount = 0;
+    bool optionsChanged = true;
+    int temporalSampleAccumulated = 0;
+    CamFrame prev{};
+    int finalBuf = 0;
+    // instrumentation: per-frame event triples (frame start, after k_initial, after the last
+    // kernel), summed only when the caller asks, so timing never synchronises a frame
+    cudaEvent_t ev[10] = {};
+    int nev = 0;
+    std::vector<std::vector<cudaEvent_t>> pendingEv;
+    std::vector<cudaEvent_t> freeEv;
+    double totalMs[4] = {0, 0, 0, 0};
+    int totalFrames = 0;
+    int launches = 0;
+    int64_t h2d = 0, d2h = 0;
+    int* status = nullptr;    // device status word
+};
+
+static void free_buffers(vr_context* c) {
+    for (int i = 0; i < 3; ++i) {
+        cudaFree(c->res[i].a); cudaFree(c->res[i].b); cudaFree(c->res[i].extra);
+        c->res[i] = vrd::ResBuf{};
+    }
+    cudaFree(c->feat[0]); cudaFree(c->feat[1]); cudaFree(c->color);
+    c->feat[0] = c->feat[1] = nullptr; c->color = nullptr;
+    c->allocMB = 0;
+}
+
+static int alloc_buffers(vr_context* c) {
+    const int mb = c->opts.mMaxBounces;
+    if (c->allocMB == mb && c->allocW == c->W && c->allocH == c->H) return VR_OK;
+    free_buffers(c);
+    size_t N = (size_t)c->W * c->H;
+    size_t ne = N * (size_t)std::max(mb - 1, 1);
+    for (int i = 0; i < 3; ++i) {
+        c->res[i].a = dalloc<float4>(N);
+        c->res[i].b = dalloc<int4>(N);
+        c->res[i].extra = dalloc<float4>(ne);
+        if (!c->res[i].a || !c->res[i].b || !c->res[i].extra) { c->err = "out of device memory (reservoirs)"; return VR_ERR_OOM; }
+        cudaMemset(c->res[i].a, 0, N * sizeof(float4));
+        cudaMemset(c->res[i].b, 0, N * sizeof(int4));
+        cudaMemset(c->res[i].extra, 0, ne * sizeof(float4));
+    }
+    for (int i = 0; i < 2; ++i) {
+        c->feat[i] = dalloc<float>(N);
+        if (!c->feat[i]) { c->err = "out of device memory (features)"; return VR_ERR_OOM; }
+        cudaMemset(c->feat[i], 0, N * sizeof(float));
+    }
+    c->color = dalloc<float>(N * 4);
+    if (!c->color) { c->err = "out of device memory (colour)"; return VR_ERR_OOM; }
+    cudaMemset(c->color, 0, N * 4 * sizeof(float));
+    c->allocMB = mb; c->allocW = c->W; c->allocH = c->H;
+    return VR_OK;
+}
+
+static bool options_valid(const vr_options* o, std::string& why) {
+    if (o->mMaxBounces < 1 || o->mMaxBounces > VR_MAX_BOUNCES) { why = "mMaxBounces must be in [1, 4]"; return false; }
+    if (o->mInitialM < 1 || o->mInitialM > 4096) { why = "mInitialM must be in [1, 4096]"; return false; }
+    if (o->mSpatialSampleCount < 1 || o->mSpatialSampleCount > 32) { why = "mSpatialSampleCount must be in [1, 32]"; return false; }
+    if (o->mSpatialReuseRounds < 1 || o->mSpatialReuseRounds > 16) { why = "mSpatialReuseRounds must be in [1, 16]"; return false; }
+    if (o->mBaselineSamplePerPixel < 1) { why = "mBaselineSamplePerPixel must be >= 1"; return false; }
+    if (o->mInitialBaseMipLevel < 0 || o->mInitialBaseMipLevel >= VR_NUM_MAX_MIPS) { why = "mInitialBaseMipLevel out of range"; return false; }
+    if (o->mInitialLightingMipLevel < 0 || o->mInitialLightingMipLevel >= VR_NUM_SLOTS) { why = "mInitialLightingMipLevel out of range"; return false; }
+    if (o->mSpatialVisibilityMipLevel < 0 || o->mSpatialVisibilityMipLevel >= VR_NUM_SLOTS) { why = "mSpatialVisibilityMipLevel out of range"; return false; }
+    if (o->mSpatialLightingMipLevel < 0 || o->mSpatialLightingMipLevel >= VR_NUM_SLOTS) { why = "mSpatialLightingMipLevel out of range"; return false; }
+    if (o->mTemporalReprojectionMipLevel < 0 || o->mTemporalReprojectionMipLevel >= VR_NUM_MAX_MIPS) { why = "mTemporalReprojectionMipLevel out of range"; return false; }
+    uint32_t methods[] = {o->mInitialLightingTrackingMethod, o->mSpatialVisibilityTrackingMethod, o->mSpatialLightingTrackingMethod,
+                          o->mFinalVisibilityTrackingMethod, o->mFinalLightTrackingMethod};
+    for (uint32_t m : methods) if (m > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown tracking method"; return false; }
+    if (o->mTemporalReprojectionMode > VR_REPROJ_NO_BACKGROUND) { why = "unknown reprojection mode"; return false; }
+    return true;
+}
+
+// every mip slot the options can reach must exist in the bound volume
+static bool slots_present(const vr_context* c, std::string& why) {
+    const vr_options& o = c->opts;
+    auto need = [&](int slot) {
+        if (slot < 0 || slot >= VR_NUM_SLOTS || !c->scene.slots[slot].valid) {
+            why = "options need mip slot " + std::to_string(slot) + " which the volume does not have";
+            return false;
+        }
+        return true;
+    };
+    int base = o.mInitialVisibilityUseLinearSampler ? o.mInitialBaseMipLevel : o.mInitialBaseMipLevel + VR_NUM_MAX_MIPS;
+    if (!need(base) || !need(o.mInitialLightingMipLevel) || !need(o.mSpatialVisibilityMipLevel) || !need(o.mSpatialLightingMipLevel) ||
+        !need(0) || !need(VR_NUM_MAX_MIPS + o.mTemporalReprojectionMipLevel))
+        return false;
+    if (o.mInitialUseCoarserGridForIndirectBounce && o.mMaxBounces > 1) {
+        int cm = std::min((base >= VR_NUM_MAX_MIPS ? VR_NUM_MAX_MIPS : 0) + c->numMips - 1, base + 1);
+        if (!need(cm)) return false;
+    }
+    return true;
+}
+
+template <int MB>
+static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st);
+
+extern "C" {
+
+void vr_options_default(vr_options* o) {
+    memset(o, 0, sizeof(*o));
+    o->mMaxBounces = 1;
+    o->mEnableTemporalReuse = 1;
+    o->mEnableSpatialReuse = 1;
+    o->mUseReference = 0;
+    o->mUseEnvironmentLights = 1;
+    o->mUseAnalyticLights = 0;
+    o->mBaselineSamplePerPixel = 1;
+    o->mVisualizeTotalTransmittance = 0;
+    o->mInitialBaseMipLevel = 1;
+    o->mInitialM = 4;
+    o->mInitialLightSamples = 1;
+    o->mInitialLightingMipLevel = 2;
+    o->mInitialVisibilityUseLinearSampler = 0;
+    o->mInitialLightingUseLinearSampler = 1;
+    o->mInitialLightingTrackingMethod = VR_TRACK_RAY_MARCHING;
+    o->mInitialVisibilityTStepScale = 1.f;
+    o->mInitialLightingTStepScale = 2.f;
+    o->mInitialUseRussianRoulette = 1;
+    o->mInitialUseCoarserGridForIndirectBounce = 1;
+    o->mTemporalReuseMThreshold = 4.f;
+    o->mTemporalReprojectionMode = VR_REPROJ_LINEAR;
+    o->mTemporalMISMethod = VR_MIS_TALBOT;
+    o->mTemporalReprojectionMipLevel = 1;
+    o->mSpatialReuseRounds = 1;
+    o->mSpatialVisibilityMipLevel = 1;
+    o->mSpatialLightingMipLevel = 1;
+    o->mSpatialVisibilityUseLinearSampler = 1;
+    o->mSpatialLightingUseLinearSampler = 1;
+    o->mSpatialVisibilityTStepScale = 1.f;
+    o->mSpatialLightingTStepScale = 1.f;
+    o->mSpatialVisibilityTrackingMethod = VR_TRACK_RAY_MARCHING;
+    o->mSpatialLightingTrackingMethod = VR_TRACK_RAY_MARCHING;
+    o->mRandomSamplerType = VR_SAMPLER_R2;
+    o->mSampleRadius = 10.f;
+    o->mSpatialSampleCount = 4;
+    o->mSpatialMISMethod = VR_MIS_TALBOT;
+    o->mFinalLightSamples = 1;
+    o->mFinalVisibilitySamples = 1;
+    o->mFinalVisibilityTrackingMethod = VR_TRACK_ANALYTIC;
+    o->mFinalLightTrackingMethod = VR_TRACK_ANALYTIC;
+    o->mFinalTStepScale = 0.2f;
+}
+
+// ---- volumes ----
+int vr_volume_create_procedural(const vr_procedural_desc* d, vr_volume** out) {
+    if (!d || !out) return VR_ERR_INVALID_ARG;
+    if (d->res <= 0 || d->res > 4096 || d->num_mips < 1 || d->num_mips > VR_NUM_MAX_MIPS || d->octaves < 1 || d->octaves > 16) return VR_ERR_INVALID_ARG;
+    if (d->res % (8 << (d->num_mips - 1)) != 0) return VR_ERR_INVALID_ARG;
+    if (!(d->voxel_size > 0.f)) return VR_ERR_INVALID_ARG;
+    try {
+        std::vector<float> g = vr::procedural_density(*d);
+        vr_volume* v = new vr_volume();
+        if (vr::build_volume(g, d->res, d->num_mips, d->world_min, d->voxel_size, d->fp16 != 0, v->v) != 0) { delete v; return VR_ERR_INVALID_ARG; }
+        *out = v;
+        return VR_OK;
+    } catch (...) {
+        return VR_ERR_OOM;
+    }
+}
+int vr_volume_create_dense(const float* density, int32_t res, int32_t num_mips, const float world_min[3], float voxel_size, int32_t fp16, vr_volume** out) {
+    if (!density || !out || !world_min) return VR_ERR_INVALID_ARG;
+    if (res <= 0 || res > 4096 || num_mips < 1 || num_mips > VR_NUM_MAX_MIPS || res % (8 << (num_mips - 1)) != 0 || !(voxel_size > 0.f)) return VR_ERR_INVALID_ARG;
+    try {
+        std::vector<float> g(density, density + (size_t)res * res * res);
+        for (float& x : g) if (!(x >= 0.f) || vr::isinf_(x)) return VR_ERR_INVALID_ARG;
+        vr_volume* v = new vr_volume();
+        if (vr::build_volume(g, res, num_mips, world_min, voxel_size, fp16 != 0, v->v) != 0) { delete v; return VR_ERR_INVALID_ARG; }
+        *out = v;
+        return VR_OK;
+    } catch (...) {
+        return VR_ERR_OOM;
+    }
+}
+void vr_volume_destroy(vr_volume* v) { delete v; }
+int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
+    if (!v || !info) return VR_ERR_INVALID_ARG;
+    memset(info, 0, sizeof(*info));
+    info->num_mips = v->v.num_mips;
+    info->res = v->v.res;
+    info->voxel_size = v->v.voxel_size;
+    info->supervoxel_diag = v->v.supervoxel_diag;
+    info->fp16 = v->v.fp16;
+    int64_t bytes = 0;
+    for (int s = 0; s < VR_NUM_SLOTS; ++s) {
+        const vr::GridSlot& g = v->v.slots[s];
+        info->num_bricks[s] = g.num_bricks;
+        if (!g.valid) continue;
+        bytes += (int64_t)g.root_child.size() * 4 + (int64_t)g.l1_vmin.size() * 4 + (int64_t)g.l1_child.size() * 4 +
+                 (int64_t)g.brick_vmin.size() * 4 + (int64_t)g.brick_bounds.size() * 4 + (int64_t)g.brick_f32.size() * 4 +
+                 (int64_t)g.brick_f16.size() * 2;
+    }
+    info->device_bytes = bytes;
+    return VR_OK;
+}
+int vr_volume_get_slot(const vr_volume* v, int32_t slot, vr_grid_view* view) {
+    if (!v || !view || slot < 0 || slot >= VR_NUM_SLOTS) return VR_ERR_INVALID_ARG;
+    vr::slot_view(v->v.slots[slot], view);
+    return VR_OK;
+}
+
+// ---- context ----
+vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int32_t* err) {
+    vr_options d;
+    if (!opts) { vr_options_default(&d); opts = &d; }
+    std::string why;
+    if (width <= 0 || height <= 0 || width > 16384 || height > 16384 || !options_valid(opts, why)) {
+        if (err) *err = VR_ERR_INVALID_ARG;
+        return nullptr;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { if (err) *err = VR_ERR_CUDA; return nullptr; }
+    vr_context* c = new vr_context();
+    c->opts = *opts;
+    c->W = width; c->H = height;
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) { delete c; if (err) *err = VR_ERR_OOM; return nullptr; }
+    cudaMemset(c->status, 0, sizeof(int));
+    c->scene.status = c->status;
+    if (err) *err = VR_OK;
+    return c;
+}
+
+void vr_destroy(vr_context* c) {
+    if (!c) return;
+    free_buffers(c);
+    for (void* p : c->sceneAllocs) cudaFree(p);
+    for (void* p : c->envAllocs) cudaFree(p);
+    for (auto& e : c->ev) if (e) cudaEventDestroy(e);
+    for (auto& v : c->pendingEv) for (auto e : v) cudaEventDestroy(e);
+    for (auto e : c->freeEv) cudaEventDestroy(e);
+    cudaFree(c->status);
+    delete c;
+}
+
+const char* vr_last_error(const vr_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int vr_set_options(vr_context* c, const vr_options* o) {
+    if (!c || !o) return VR_ERR_INVALID_ARG;
+    std::string why;
+    if (!options_valid(o, why)) { c->err = why; return VR_ERR_INVALID_ARG; }
+    c->opts = *o;
+    c->optionsChanged = true;
+    return VR_OK;
+}
+int vr_get_options(const vr_context* c, vr_options* o) {
+    if (!c || !o) return VR_ERR_INVALID_ARG;
+    *o = c->opts;
+    return VR_OK;
+}
+int vr_resize(vr_context* c, int32_t w, int32_t h) {
+    if (!c || w <= 0 || h <= 0 || w > 16384 || h > 16384) return VR_ERR_INVALID_ARG;
+    c->W = w; c->H = h;
+    c->optionsChanged = true;
+    return VR_OK;
+}
+
+// ---- scene binding ----
+int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
+    if (!c || !vol || !m) return VR_ERR_INVALID_ARG;
+    if (!(m->sigma_s[0] + m->sigma_a[0] > 0.f)) { c->err = "sigma_t must be positive"; return VR_ERR_INVALID_ARG; }
+    if (m->sigma_s[0] + m->sigma_a[0] != m->sigma_s[1] + m->sigma_a[1] || m->sigma_s[1] + m->sigma_a[1] != m->sigma_s[2] + m->sigma_a[2]) {
+        c->err = "sigma_t must be grey (sigma_s + sigma_a equal on all channels)"; return VR_ERR_INVALID_ARG;
+    }
+    for (void* p : c->sceneAllocs) cudaFree(p);
+    c->sceneAllocs.clear();
+    const vr::Volume& v = vol->v;
+    for (int s = 0; s < VR_NUM_SLOTS; ++s) {
+        vrd::DevSlot& d = c->scene.slots[s];
+        memset(&d, 0, sizeof(d));
+        const vr::GridSlot& g = v.slots[s];
+        if (!g.valid) continue;
+        auto up = [&](const void* src, size_t bytes) -> void* {
+            void* p = nullptr;
+            if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+            c->sceneAllocs.push_back(p);
+            if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+            return p;
+        };
+        d.valid = 1;
+        d.res = g.res;
+        d.bmaxf = (float)g.res;
+        d.maxValue = g.max_value;
+        memcpy(d.M, g.world_to_index, sizeof(d.M));
+        d.root = (const int*)up(g.root_child.data(), g.root_child.size() * 4);
+        d.l1vmin = (const int4*)up(g.l1_vmin.data(), g.l1_vmin.size() * 4);
+        d.l1child = (const int*)up(g.l1_child.data(), g.l1_child.size() * 4);
+        d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
+        d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
+        if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
+        else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+        if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) { c->err = "out of device memory (volume)"; return VR_ERR_OOM; }
+    }
+    c->scene.sigma_s = mk3(m->sigma_s[0], m->sigma_s[1], m->sigma_s[2]);
+    c->scene.sigma_a = mk3(m->sigma_a[0], m->sigma_a[1], m->sigma_a[2]);
+    c->scene.sigma_t = m->sigma_s[0] + m->sigma_a[0];
+    c->scene.g = m->g;
+    c->scene.dscale = m->density_scale;
+    c->scene.tStep = v.voxel_size;
+    c->scene.superDiag = v.supervoxel_diag;
+    c->scene.numMips = v.num_mips;
+    c->numMips = v.num_mips;
+    c->hasVolume = true;
+    c->optionsChanged = true;
+    return VR_OK;
+}
+
+int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const vr_env_map* env) {
+    if (!c || n < 0 || n > vrd::kMaxLights || (n > 0 && !lights)) { if (c) c->err = "at most 64 point lights"; return VR_ERR_INVALID_ARG; }
+    c->scene.numLights = n;
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) { c->scene.lightPos[i][k] = lights[i].pos[k]; c->scene.lightI[i][k] = lights[i].intensity[k]; }
+    for (void* p : c->envAllocs) cudaFree(p);
+    c->envAllocs.clear();
+    c->scene.hasEnv = env != nullptr;
+    if (env) {
+        if (!env->rgb || env->width <= 0 || env->height <= 0) { c->err = "invalid environment map"; return VR_ERR_INVALID_ARG; }
+        HostEnv& e = c->env;
+        e.w = env->width; e.h = env->height;
+        e.rgb.assign(env->rgb, env->rgb + (size_t)e.w * e.h * 3);
+        build_importance(e);
+        float *drgb = nullptr, *dimp = nullptr;
+        if (cudaMalloc(&drgb, e.rgb.size() * 4) != cudaSuccess || cudaMalloc(&dimp, e.imp.size() * 4) != cudaSuccess) { c->err = "out of device memory (env)"; return VR_ERR_OOM; }
+        c->envAllocs.push_back(drgb); c->envAllocs.push_back(dimp);
+        cudaMemcpy(drgb, e.rgb.data(), e.rgb.size() * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dimp, e.imp.data(), e.imp.size() * 4, cudaMemcpyHostToDevice);
+        c->scene.envRGB = drgb;
+        c->scene.envW = e.w; c->scene.envH = e.h;
+        c->scene.envScale = mk3(env->scale[0], env->scale[1], env->scale[2]);
+        memcpy(c->scene.envRot, env->rotation, sizeof(c->scene.envRot));
+        for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) c->scene.envInv[i * 3 + j] = env->rotation[j * 3 + i];
+        c->scene.imp = dimp;
+        memcpy(c->scene.impOff, e.off, sizeof(e.off));
+        c->scene.impDim = 512;
+        c->scene.impBaseMip = 9;
+    }
+    c->optionsChanged = true;
+    return VR_OK;
+}
+
+static void fill_sampling(vrd::SamplingOptions& s, uint32_t vm, uint32_t lm, int ls, int lmip, int vs, int vmip, int vlin, int llin,
+                          float vts, float lts, const vr_options& o) {
+    s.visibilityTrackingMethod = vm; s.lightingTrackingMethod = lm;
+    s.lightSamples = ls; s.lightingMipLevel = lmip; s.visibilitySamples = vs; s.visibilityMipLevel = vmip;
+    s.visibilityUseLinearSampler = vlin; s.lightingUseLinearSampler = llin;
+    s.visibilityTStepScale = vts; s.lightingTStepScale = lts;
+    s.useEnvironmentLights = o.mUseEnvironmentLights; s.useAnalyticLights = o.mUseAnalyticLights;
+}
+
+static vrd::FrameParams frame_params(vr_context* c, const CamFrame& cam, int numTotalRounds) {
+    const vr_options& o = c->opts;
+    vrd::FrameParams P;
+    memset(&P, 0, sizeof(P));
+    P.W = c->W; P.H = c->H; P.N = c->W * c->H;
+    P.maxBounces = o.mMaxBounces;
+    P.frameCount = c->frameCount;
+    P.numTotalRounds = numTotalRounds;
+    P.noReuse = !o.mEnableSpatialReuse && !o.mEnableTemporalReuse;
+    P.initialM = o.mInitialM;
+    P.baselineSpp = o.mBaselineSamplePerPixel;
+    P.useRR = o.mInitialUseRussianRoulette;
+    P.useCoarser = o.mInitialUseCoarserGridForIndirectBounce;
+    P.temporalEnabled = o.mEnableTemporalReuse && !o.mUseReference;
+    P.isFirstFrame = c->temporalSampleAccumulated == 0;
+    P.reprojMode = (int)o.mTemporalReprojectionMode;
+    P.temporalTalbot = o.mTemporalMISMethod == VR_MIS_TALBOT;
+    P.reprojMip = o.mTemporalReprojectionMipLevel;
+    P.temporalMThreshold = o.mTemporalReuseMThreshold;
+    P.spatialTalbot = o.mSpatialMISMethod == VR_MIS_TALBOT;
+    P.spatialK = o.mSpatialSampleCount;
+    P.spatialRounds = o.mSpatialReuseRounds;
+    P.visualizeTr = o.mVisualizeTotalTransmittance;
+    fill_sampling(P.initial, VR_TRACK_ANALYTIC, o.mInitialLightingTrackingMethod, o.mInitialLightSamples, o.mInitialLightingMipLevel, 1,
+                  o.mInitialVisibilityUseLinearSampler ? o.mInitialBaseMipLevel : o.mInitialBaseMipLevel + VR_NUM_MAX_MIPS,
+                  o.mInitialVisibilityUseLinearSampler != 0, o.mInitialLightingUseLinearSampler != 0, o.mInitialVisibilityTStepScale,
+                  o.mInitialLightingTStepScale, o);
+    fill_sampling(P.spatial, o.mSpatialVisibilityTrackingMethod, o.mSpatialLightingTrackingMethod, 1, o.mSpatialLightingMipLevel, 1,
+                  o.mSpatialVisibilityMipLevel, o.mSpatialVisibilityUseLinearSampler != 0, o.mSpatialLightingUseLinearSampler != 0,
+                  o.mSpatialVisibilityTStepScale, o.mSpatialLightingTStepScale, o);
+    bool flA = o.mFinalLightTrackingMethod == VR_TRACK_ANALYTIC || o.mFinalLightTrackingMethod == VR_TRACK_RAY_MARCHING;
+    bool fvA = o.mFinalVisibilityTrackingMethod == VR_TRACK_ANALYTIC || o.mFinalVisibilityTrackingMethod == VR_TRACK_RAY_MARCHING;
+    fill_sampling(P.fin, o.mFinalVisibilityTrackingMethod, o.mFinalLightTrackingMethod, flA ? 1 : o.mFinalLightSamples, 0,
+                  fvA ? 1 : o.mFinalVisibilitySamples, 0, 1, 1, o.mFinalTStepScale, o.mFinalTStepScale, o);
+    P.camPos = cam.pos; P.camU = cam.U; P.camV = cam.V; P.camW = cam.W;
+    P.prevPos = c->prev.pos; P.prevU = c->prev.U; P.prevV = c->prev.V; P.prevW = c->prev.W;
+    memcpy(P.prevView, c->prev.view, sizeof(P.prevView));
+    memcpy(P.prevProj, c->prev.proj, sizeof(P.prevProj));
+    return P;
+}
+
+static int check_cuda(vr_context* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { c->err = std::string(what) + ": " + cudaGetErrorString(e); return VR_ERR_CUDA; }
+    return VR_OK;
+}
+
+static int prepare_frame(vr_context* c, const vr_camera* cam) {
+    if (!cam) return VR_ERR_INVALID_ARG;
+    if (!c->hasVolume) { c->err = "no volume bound (vr_set_volume)"; return VR_ERR_STATE; }
+    std::string why;
+    if (!slots_present(c, why)) { c->err = why; return VR_ERR_INVALID_ARG; }
+    if (c->opts.mUseAnalyticLights && c->scene.numLights == 0) { c->err = "mUseAnalyticLights needs at least one point light"; return VR_ERR_INVALID_ARG; }
+    if (c->opts.mUseEnvironmentLights && !c->scene.hasEnv) { c->err = "mUseEnvironmentLights needs an environment map"; return VR_ERR_INVALID_ARG; }
+    int r = alloc_buffers(c);
+    if (r) return r;
+    if (c->optionsChanged) { c->frameCount = 0; c->temporalSampleAccumulated = 0; c->optionsChanged = false; }
+    return VR_OK;
+}
+
+static int upload_scene(vr_context* c, cudaStream_t st) {
+    cudaError_t e;
+    switch (c->opts.mMaxBounces) {
+        case 1: e = vrk::upload_scene_1(c->scene, st); break;
+        case 2: e = vrk::upload_scene_2(c->scene, st); break;
+        case 3: e = vrk::upload_scene_3(c->scene, st); break;
+        default: e = vrk::upload_scene_4(c->scene, st); break;
+    }
+    if (e != cudaSuccess) { c->err = std::string("scene upload: ") + cudaGetErrorString(e); return VR_ERR_CUDA; }
+    return VR_OK;
+}
+
+int vr_render_frame(vr_context* c, const vr_camera* cam, float* out_rgba, float* out_mvec, void* stream) {
+    if (!c || !out_rgba) return VR_ERR_INVALID_ARG;
+    int r = prepare_frame(c, cam);
+    if (r) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((r = upload_scene(c, st))) return r;
+    const vr_options& o = c->opts;
+    CamFrame cf = camera_frame(*cam, c->W, c->H);
+    int numTotalRounds = (o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0) + o.mEnableTemporalReuse + 1 + 1;
+    vrd::FrameParams P = frame_params(c, cf, numTotalRounds);
+    vrd::FrameBuffers B;
+    memset(&B, 0, sizeof(B));
+    B.cur = c->res[0];
+    B.sp[0] = c->res[0];
+    B.sp[1] = c->res[1];
+    B.hist = c->res[2];
+    B.featCur = c->feat[c->featCurIdx];
+    B.featPrev = c->feat[c->featCurIdx ^ 1];
+    B.color = o.mUseReference ? c->color : nullptr;
+    B.out = (float4*)out_rgba;
+    B.mvec = (float2*)out_mvec;
+    c->nev = 0;
+    c->launches = 0;
+    c->d2h = 0;
+    switch (o.mMaxBounces) {
+        case 1: launch_frame_kernels<1>(c, P, B, st); break;
+        case 2: launch_frame_kernels<2>(c, P, B, st); break;
+        case 3: launch_frame_kernels<3>(c, P, B, st); break;
+        default: launch_frame_kernels<4>(c, P, B, st); break;
+    }
+    if ((r = check_cuda(c, "frame kernels"))) return r;
+    c->h2d = (int64_t)sizeof(vrd::DevScene) + (int64_t)c->launches * (int64_t)(sizeof(vrd::FrameParams) + sizeof(vrd::FrameBuffers)) +
+             (o.mEnableSpatialReuse && !o.mUseReference ? (int64_t)o.mSpatialReuseRounds * (int64_t)sizeof(vrd::SpatialParams) : 0);
+    if (!o.mUseReference && o.mEnableTemporalReuse) c->featCurIdx ^= 1;
+    c->temporalSampleAccumulated = 1;
+    c->prev = cf;
+    c->frameCount++;
+    return VR_OK;
+}
+
+int vr_render_frame_host(vr_context* c, const vr_camera* cam, float* out_rgba_host, void* stream) {
+    if (!c || !out_rgba_host) return VR_ERR_INVALID_ARG;
+    size_t bytes = (size_t)c->W * c->H * 16;
+    float* d = nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    static thread_local std::vector<std::pair<size_t, float*>> scratch;
+    for (auto& s : scratch) if (s.first == bytes) d = s.second;
+    if (!d) {
+        if (cudaMalloc(&d, bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
+        scratch.push_back({bytes, d});
+    }
+    int r = vr_render_frame(c, cam, d, nullptr, stream);
+    if (r) return r;
+    cudaMemcpyAsync(out_rgba_host, d, bytes, cudaMemcpyDeviceToHost, st);
+    c->d2h = (int64_t)bytes;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return check_cuda(c, "frame");
+    int status = 0;
+    cudaMemcpy(&status, c->status, 4, cudaMemcpyDeviceToHost);
+    if (status) {
+        int zero = 0;
+        cudaMemcpy(c->status, &zero, 4, cudaMemcpyHostToDevice);
+        c->err = "a bounded device loop hit its iteration limit";
+        return VR_ERR_LOOP_LIMIT;
+    }
+    return VR_OK;
+}
+
+int vr_render_reference(vr_context* c, const vr_camera* cam, int32_t first_frame, int32_t num_frames, double* accum, void* stream) {
+    if (!c || !accum || num_frames < 0) return VR_ERR_INVALID_ARG;
+    int r = prepare_frame(c, cam);
+    if (r) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    if ((r = upload_scene(c, st))) return r;
+    const vr_options& o = c->opts;
+    CamFrame cf = camera_frame(*cam, c->W, c->H);
+    int numTotalRounds = (o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0) + o.mEnableTemporalReuse + 1 + 1;
+    vrd::FrameParams P = frame_params(c, cf, numTotalRounds);
+    dim3 grid((c->W + 7) / 8, (c->H + 15) / 16), block(128);
+    // chunks of frames keep each launch short
+    for (int f = 0; f < num_frames; f += 16) {
+        int cnt = std::min(16, num_frames - f);
+        switch (o.mMaxBounces) {
+            case 1: vrk::launch_reference_1(P, first_frame + f, cnt, accum, grid, block, st); break;
+            case 2: vrk::launch_reference_2(P, first_frame + f, cnt, accum, grid, block, st); break;
+            case 3: vrk::launch_reference_3(P, first_frame + f, cnt, accum, grid, block, st); break;
+            default: vrk::launch_reference_4(P, first_frame + f, cnt, accum, grid, block, st); break;
+        }
+    }
+    return check_cuda(c, "reference");
+}
+
+// ---- exports ----
+int32_t vr_reservoir_bytes(const vr_context* c) { return c ? (c->opts.mMaxBounces > 1 ? 36 : 32) : 0; }
+
+int vr_export_reservoirs(vr_context* c, int32_t which, void* host, size_t bytes) {
+    if (!c || !host || which < 0 || which > 3) return VR_ERR_INVALID_ARG;
+    size_t N = (size_t)c->W * c->H;
+    int rb = vr_reservoir_bytes(c);
+    if (bytes < N * rb) return VR_ERR_INVALID_ARG;
+    if (!c->res[0].a) { c->err = "no frame rendered yet"; return VR_ERR_STATE; }
+    int idx = which == 0 ? c->finalBuf : (which == 1 ? 2 : which - 2);
+    std::vector<float4> a(N);
+    std::vector<int4> b(N);
+    cudaDeviceSynchronize();
+    cudaMemcpy(a.data(), c->res[idx].a, N * 16, cudaMemcpyDeviceToHost);
+    cudaMemcpy(b.data(), c->res[idx].b, N * 16, cudaMemcpyDeviceToHost);
+    int mb = c->opts.mMaxBounces;
+    char* o = (char*)host;
+    for (size_t i = 0; i < N; ++i) {
+        vr_reservoir_aos r;
+        r.runningSum = a[i].x; r.M = a[i].y; r.depth = a[i].z; r.p_y = a[i].w;
+        memcpy(&r.lightUV[0], &b[i].x, 4); memcpy(&r.lightUV[1], &b[i].y, 4);
+        r.lightID = b[i].z; r.sampledPixel = b[i].w;
+        r.extraBounceStartId = (int32_t)(i * (size_t)(mb - 1));
+        memcpy(o + i * rb, &r, rb);
+    }
+    return check_cuda(c, "export");
+}
+
+int vr_export_extra_bounces(vr_context* c, int32_t which, float* host, size_t bytes) {
+    if (!c || !host || which < 0 || which > 3) return VR_ERR_INVALID_ARG;
+    size_t N = (size_t)c->W * c->H;
+    int mb = c->opts.mMaxBounces;
+    size_t ne = N * (size_t)std::max(mb - 1, 0);
+    if (bytes < ne * 12) return VR_ERR_INVALID_ARG;
+    if (ne == 0) return VR_OK;
+    int idx = which == 0 ? c->finalBuf : (which == 1 ? 2 : which - 2);
+    std::vector<float4> e(ne);
+    cudaDeviceSynchronize();
+    cudaMemcpy(e.data(), c->res[idx].extra, ne * 16, cudaMemcpyDeviceToHost);
+    // device planes are b*N + pixel; the reference layout is pixel*(mb-1) + b
+    for (size_t p = 0; p < N; ++p)
+        for (int b = 0; b < mb - 1; ++b) {
+            const float4& v = e[(size_t)b * N + p];
+            float* d = host + (p * (mb - 1) + b) * 3;
+            d[0] = v.x; d[1] = v.y; d[2] = v.z;
+        }
+    return check_cuda(c, "export extra");
+}
+
+int vr_export_features(vr_context* c, void* host, size_t bytes) {
+    if (!c || !host) return VR_ERR_INVALID_ARG;
+    size_t N = (size_t)c->W * c->H;
+    if (bytes < N * 8) return VR_ERR_INVALID_ARG;
+    if (!c->feat[0]) return VR_ERR_STATE;
+    std::vector<float> f(N);
+    cudaDeviceSynchronize();
+    // the features of the last frame: the buffer before the end-of-frame swap
+    bool swapped = !c->opts.mUseReference && c->opts.mEnableTemporalReuse;
+    int idx = swapped ? (c->featCurIdx ^ 1) : c->featCurIdx;
+    cudaMemcpy(f.data(), c->feat[idx], N * 4, cudaMemcpyDeviceToHost);
+    int32_t* o = (int32_t*)host;
+    for (size_t i = 0; i < N; ++i) { o[i * 2] = 1; memcpy(&o[i * 2 + 1], &f[i], 4); }
+    return check_cuda(c, "export features");
+}
+
+int32_t vr_frame_count(const vr_context* c) { return c ? c->frameCount : -1; }
+
+int vr_last_timings(const vr_context* c, float* ms, int32_t max_entries, int32_t* n) {
+    if (!c || !ms || !n) return VR_ERR_INVALID_ARG;
+    int k = 0;
+    for (int i = 0; i + 1 < c->nev && k < max_entries; ++i) {
+        cudaEventSynchronize(c->ev[i + 1]);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, c->ev[i], c->ev[i + 1]);
+        ms[k++] = t;
+    }
+    *n = k;
+    return VR_OK;
+}
+int32_t vr_last_launch_count(const vr_context* c) { return c ? c->launches : 0; }
+
+static void drain_events(vr_context* c) {
+    for (auto& v : c->pendingEv) {
+        cudaEventSynchronize(v.back());
+        for (size_t i = 0; i + 1 < v.size() && i < 4; ++i) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, v[i], v[i + 1]);
+            c->totalMs[i] += t;
+        }
+        c->totalFrames++;
+        for (auto e : v) c->freeEv.push_back(e);
+    }
+    c->pendingEv.clear();
+}
+int vr_kernel_time_totals(vr_context* c, float* ms, int32_t max_entries, int32_t* frames, int32_t reset) {
+    if (!c || !ms || !frames) return VR_ERR_INVALID_ARG;
+    drain_events(c);
+    for (int i = 0; i < max_entries && i < 4; ++i) ms[i] = (float)c->totalMs[i];
+    *frames = c->totalFrames;
+    if (reset) { for (double& t : c->totalMs) t = 0; c->totalFrames = 0; }
+    return VR_OK;
+}
+int vr_last_transfer_bytes(const vr_context* c, int64_t* h2d, int64_t* d2h) {
+    if (!c || !h2d || !d2h) return VR_ERR_INVALID_ARG;
+    *h2d = c->h2d;
+    *d2h = c->d2h;
+    return VR_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// frame launch sequence (VolumetricReSTIR.cpp:499-762)
+// ---------------------------------------------------------------------------------------
+template <int MB>
+static void launch_initial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, dim3 g, dim3 b, cudaStream_t st) {
+    if (MB == 1) vrk::launch_initial_1(P, B, g, b, st);
+    else if (MB == 2) vrk::launch_initial_2(P, B, g, b, st);
+    else if (MB == 3) vrk::launch_initial_3(P, B, g, b, st);
+    else vrk::launch_initial_4(P, B, g, b, st);
+}
+template <int MB>
+static void launch_spatial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st) {
+    if (MB == 1) vrk::launch_spatial_1(P, B, S, g, b, st);
+    else if (MB == 2) vrk::launch_spatial_2(P, B, S, g, b, st);
+    else if (MB == 3) vrk::launch_spatial_3(P, B, S, g, b, st);
+    else vrk::launch_spatial_4(P, B, S, g, b, st);
+}
+template <int MB>
+static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, int wh, dim3 g, dim3 b, cudaStream_t st) {
+    if (MB == 1) vrk::launch_final_1(P, B, wh, g, b, st);
+    else if (MB == 2) vrk::launch_final_2(P, B, wh, g, b, st);
+    else if (MB == 3) vrk::launch_final_3(P, B, wh, g, b, st);
+    else vrk::launch_final_4(P, B, wh, g, b, st);
+}
+
+template <int MB>
+static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st) {
+    const vr_options& o = c->opts;
+    dim3 grid((c->W + 7) / 8, (c->H + 15) / 16), block(128);
+    std::vector<cudaEvent_t> frameEv;
+    auto mark = [&]() {
+        if (c->nev < 10) cudaEventRecord(c->ev[c->nev++], st);
+        cudaEvent_t e;
+        if (!c->freeEv.empty()) { e = c->freeEv.back(); c->freeEv.pop_back(); }
+        else cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        frameEv.push_back(e);
+    };
+    mark();
+    launch_initial<MB>(P, B, grid, block, st);
+    c->launches++;
+    mark();
+    int totalRoundId = 0;
+    bool temporal = !o.mUseReference && o.mEnableTemporalReuse;
+    bool spatial = !o.mUseReference && o.mEnableSpatialReuse;
+    size_t N = (size_t)c->W * c->H;
+    if (temporal && !spatial) {
+        // copyResource(temporal <- perPixel[0]) (VolumetricReSTIR.cpp:632-637)
+        cudaMemcpyAsync(c->res[2].a, c->res[0].a, N * 16, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(c->res[2].b, c->res[0].b, N * 16, cudaMemcpyDeviceToDevice, st);
+        if (o.mMaxBounces > 1)
+            cudaMemcpyAsync(c->res[2].extra, c->res[0].extra, N * (size_t)(o.mMaxBounces - 1) * 16, cudaMemcpyDeviceToDevice, st);
+    }
+    if (spatial) {
+        for (int r = 0; r < o.mSpatialReuseRounds; ++r) {
+            vrd::SpatialParams S;
+            memset(&S, 0, sizeof(S));
+            S.in = totalRoundId % 2;
+            S.out = (totalRoundId + 1) % 2;
+            int roundOffset = o.mEnableTemporalReuse + 1;
+            S.roundId = r;
+            S.numRounds = o.mSpatialReuseRounds + roundOffset + 1;
+            S.rid = r + roundOffset;
+            S.last = r == o.mSpatialReuseRounds - 1;
+            S.writeHistory = temporal;
+            int r2 = ((o.mSpatialReuseRounds + 1) * c->frameCount + r) % 16;
+            neighbor_offsets(o, r2, S.offs);
+            launch_spatial<MB>(P, B, S, grid, block, st);
+            c->launches++;
+            totalRoundId++;
+            if (S.last) mark();
+        }
+    } else {
+        launch_final<MB>(P, B, 0, grid, block, st);
+        c->launches++;
+        mark();
+    }
+    c->finalBuf = totalRoundId % 2;
+    c->pendingEv.push_back(frameEv);
+    if (c->pendingEv.size() > 512) drain_events(c);
+}
+
+// ---------------------------------------------------------------------------------------
+// self tests
+// ---------------------------------------------------------------------------------------
+#if !defined(VR_HOST_EMULATION)
+__global__ void k_selftest_math(int op, const float* a, const float* b, float* out, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float x = a[i], y = b ? b[i] : 0.f, r = 0.f;
+    switch (op) {
+        case 0: r = vr::exp_(x); break;
+        case 1: r = vr::log_(x); break;
+        case 2: r = vr::sin_(x); break;
+        case 3: r = vr::cos_(x); break;
+        case 4: r = vr::atan2_(x, y); break;
+        case 5: r = vr::acos_(x); break;
+        case 6: r = vr::pow_(x, y); break;
+        default: r = vr::sqrt_(x); break;
+    }
+    out[i] = r;
+}
+__global__ void k_selftest_rng(const uint32_t* cases, int n, int draws, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vr::Rng r = vr::rng_create(cases[i * 3], cases[i * 3 + 1], cases[i * 3 + 2]);
+    for (int j = 0; j < draws; ++j) out[(size_t)i * draws + j] = vr::next1D(r);
+}
+
+extern "C" int vr_selftest_math(int32_t op, const float* a, const float* b, float* out, int32_t n) {
+    if (!a || !out || n <= 0 || op < 0 || op > 7) return VR_ERR_INVALID_ARG;
+    float *da, *db = nullptr, *dout;
+    if (cudaMalloc(&da, n * 4) != cudaSuccess) return VR_ERR_CUDA;
+    cudaMalloc(&dout, n * 4);
+    cudaMemcpy(da, a, n * 4, cudaMemcpyHostToDevice);
+    if (b) { cudaMalloc(&db, n * 4); cudaMemcpy(db, b, n * 4, cudaMemcpyHostToDevice); }
+    k_selftest_math<<<(n + 255) / 256, 256>>>(op, da, db, dout, n);
+    cudaMemcpy(out, dout, n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(da); cudaFree(db); cudaFree(dout);
+    return cudaGetLastError() == cudaSuccess ? VR_OK : VR_ERR_CUDA;
+}
+extern "C" int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out) {
+    if (!cases || !out || n <= 0 || draws <= 0) return VR_ERR_INVALID_ARG;
+    uint32_t* dc; float* dout;
+    if (cudaMalloc(&dc, (size_t)n * 12) != cudaSuccess) return VR_ERR_CUDA;
+    cudaMalloc(&dout, (size_t)n * draws * 4);
+    cudaMemcpy(dc, cases, (size_t)n * 12, cudaMemcpyHostToDevice);
+    k_selftest_rng<<<(n + 127) / 128, 128>>>(dc, n, draws, dout);
+    cudaMemcpy(out, dout, (size_t)n * draws * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dc); cudaFree(dout);
+    return cudaGetLastError() == cudaSuccess ? VR_OK : VR_ERR_CUDA;
+}
+#endif  // !VR_HOST_EMULATION
+
+// ---------------------------------------------------------------------------------------
+// checkpoint / resume of the history (all device buffers + frame counter + previous camera)
+// ---------------------------------------------------------------------------------------
+namespace {
+struct StateHeader {
+    uint32_t magic, version;
+    int32_t W, H, maxBounces, frameCount, temporalSampleAccumulated, featCurIdx, finalBuf, optionsChanged;
+    CamFrame prev;
+};
+constexpr uint32_t kStateMagic = 0x56525354u;   // "VRST"
+}
+extern "C" int64_t vr_state_bytes(const vr_context* c) {
+    if (!c) return 0;
+    int64_t N = (int64_t)c->W * c->H;
+    int64_t ne = N * std::max(c->opts.mMaxBounces - 1, 1);
+    return (int64_t)sizeof(StateHeader) + 3 * (N * 32 + ne * 16) + 2 * N * 4 + N * 16;
+}
+extern "C" int vr_export_state(vr_context* c, void* host, size_t bytes) {
+    if (!c || !host || (int64_t)bytes < vr_state_bytes(c)) return VR_ERR_INVALID_ARG;
+    int r = alloc_buffers(c);
+    if (r) return r;
+    size_t N = (size_t)c->W * c->H, ne = N * (size_t)std::max(c->opts.mMaxBounces - 1, 1);
+    StateHeader h{kStateMagic, 1, c->W, c->H, c->opts.mMaxBounces, c->frameCount, c->temporalSampleAccumulated,
+                  c->featCurIdx, c->finalBuf, c->optionsChanged ? 1 : 0, c->prev};
+    char* p = (char*)host;
+    memcpy(p, &h, sizeof(h)); p += sizeof(h);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < 3; ++i) {
+        cudaMemcpy(p, c->res[i].a, N * 16, cudaMemcpyDeviceToHost); p += N * 16;
+        cudaMemcpy(p, c->res[i].b, N * 16, cudaMemcpyDeviceToHost); p += N * 16;
+        cudaMemcpy(p, c->res[i].extra, ne * 16, cudaMemcpyDeviceToHost); p += ne * 16;
+    }
+    for (int i = 0; i < 2; ++i) { cudaMemcpy(p, c->feat[i], N * 4, cudaMemcpyDeviceToHost); p += N * 4; }
+    cudaMemcpy(p, c->color, N * 16, cudaMemcpyDeviceToHost);
+    return check_cuda(c, "export state");
+}
+extern "C" int vr_import_state(vr_context* c, const void* host, size_t bytes) {
+    if (!c || !host || (int64_t)bytes < (int64_t)sizeof(StateHeader)) return VR_ERR_INVALID_ARG;
+    StateHeader h;
+    memcpy(&h, host, sizeof(h));
+    if (h.magic != kStateMagic || h.version != 1 || h.W != c->W || h.H != c->H || h.maxBounces != c->opts.mMaxBounces) {
+        c->err = "state blob does not match this context (size or max path length)";
+        return VR_ERR_INVALID_ARG;
+    }
+    if ((int64_t)bytes < vr_state_bytes(c)) return VR_ERR_INVALID_ARG;
+    int r = alloc_buffers(c);
+    if (r) return r;
+    size_t N = (size_t)c->W * c->H, ne = N * (size_t)std::max(c->opts.mMaxBounces - 1, 1);
+    const char* p = (const char*)host + sizeof(h);
+    for (int i = 0; i < 3; ++i) {
+        cudaMemcpy(c->res[i].a, p, N * 16, cudaMemcpyHostToDevice); p += N * 16;
+        cudaMemcpy(c->res[i].b, p, N * 16, cudaMemcpyHostToDevice); p += N * 16;
+        cudaMemcpy(c->res[i].extra, p, ne * 16, cudaMemcpyHostToDevice); p += ne * 16;
+    }
+    for (int i = 0; i < 2; ++i) { cudaMemcpy(c->feat[i], p, N * 4, cudaMemcpyHostToDevice); p += N * 4; }
+    cudaMemcpy(c->color, p, N * 16, cudaMemcpyHostToDevice);
+    c->frameCount = h.frameCount;
+    c->temporalSampleAccumulated = h.temporalSampleAccumulated;
+    c->featCurIdx = h.featCurIdx;
+    c->finalBuf = h.finalBuf;
+    c->optionsChanged = h.optionsChanged != 0;
+    c->prev = h.prev;
+    return check_cuda(c, "import state");
+}

@@ -1,0 +1,32 @@
+// frame_kernels.cu -- instantiates the frame-loop kernels for one maximum path length.
+// Compiled once per VR_MB in {1, 2, 3, 4} so the four variants build in parallel; each
+// object has its own copy of the scene constants, uploaded by upload_scene_<MB>.
+#include <cuda_runtime.h>
+
+#include "vr_kernels.cuh"
+
+#ifndef VR_MB
+#error "VR_MB must be defined (1..4)"
+#endif
+#define VR_CAT2(a, b) a##b
+#define VR_CAT(a, b) VR_CAT2(a, b)
+
+namespace vrk {
+
+cudaError_t VR_CAT(upload_scene_, VR_MB)(const vrd::DevScene& s, cudaStream_t st) {
+    return cudaMemcpyToSymbolAsync(vrd::c_scene, &s, sizeof(vrd::DevScene), 0, cudaMemcpyHostToDevice, st);
+}
+void VR_CAT(launch_initial_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, dim3 g, dim3 b, cudaStream_t st) {
+    vrd::k_initial<VR_MB><<<g, b, 0, st>>>(P, B);
+}
+void VR_CAT(launch_spatial_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st) {
+    vrd::k_spatial<VR_MB><<<g, b, 0, st>>>(P, B, S);
+}
+void VR_CAT(launch_final_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, int writeHist, dim3 g, dim3 b, cudaStream_t st) {
+    vrd::k_final<VR_MB><<<g, b, 0, st>>>(P, B, writeHist);
+}
+void VR_CAT(launch_reference_, VR_MB)(const vrd::FrameParams& P, int first, int count, double* accum, dim3 g, dim3 b, cudaStream_t st) {
+    vrd::k_reference<VR_MB><<<g, b, 0, st>>>(P, first, count, accum);
+}
+
+}  // namespace vrk

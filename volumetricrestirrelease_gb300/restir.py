@@ -1,0 +1,211 @@
+"""Host-side mirror of the reference render pass interface.
+
+`VolumetricReSTIR` keeps the names and behaviour of the reference's pass
+(Source/RenderPasses/VolumetricReSTIR/VolumetricReSTIR.h:36-315):
+
+  * construction from a parameter dictionary (VolumetricReSTIR::create, .cpp:61-70); unknown
+    keys produce a warning, as serializePass does (.h:305-311);
+  * `mParams` / `setParams` with the VolumetricReSTIRParams field names; any change resets the
+    temporal history like mOptionsChanged (.cpp:349-359);
+  * `setScene` binds the volume, medium, lights and environment (.cpp:1218-1256);
+  * `execute` renders one frame into a device RGBA32F buffer (`accumulated_color`).
+
+All rendering goes through libvrestir.so (CUDA); PyTorch only provides device buffers and the
+current stream.
+"""
+import ctypes as C
+import warnings
+
+import numpy as np
+
+from . import capi
+
+
+class Volume:
+    """Host-side sparse brick grid with its mip pyramids (owned by the library)."""
+
+    def __init__(self, handle, lib):
+        self._h = handle
+        self._lib = lib
+
+    @classmethod
+    def procedural(cls, desc, lib=None):
+        lib = lib or capi.load()
+        h = C.c_void_p()
+        r = lib.vr_volume_create_procedural(C.byref(desc), C.byref(h))
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_create_procedural failed ({r})")
+        return cls(h, lib)
+
+    @classmethod
+    def dense(cls, density, world_min, voxel_size, num_mips=4, fp16=False, lib=None):
+        lib = lib or capi.load()
+        d = np.ascontiguousarray(density, dtype=np.float32)
+        assert d.ndim == 3 and d.shape[0] == d.shape[1] == d.shape[2]
+        wm = (C.c_float * 3)(*world_min)
+        h = C.c_void_p()
+        r = lib.vr_volume_create_dense(d.ctypes.data_as(C.POINTER(C.c_float)), d.shape[0], num_mips, wm,
+                                       voxel_size, 1 if fp16 else 0, C.byref(h))
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_create_dense failed ({r})")
+        return cls(h, lib)
+
+    def info(self):
+        i = capi.VolumeInfo()
+        self._lib.vr_volume_get_info(self._h, C.byref(i))
+        return i
+
+    def slot(self, s):
+        v = capi.GridView()
+        self._lib.vr_volume_get_slot(self._h, s, C.byref(v))
+        return v
+
+    def views(self):
+        arr = (capi.GridView * capi.VR_NUM_SLOTS)()
+        for s in range(capi.VR_NUM_SLOTS):
+            self._lib.vr_volume_get_slot(self._h, s, C.byref(arr[s]))
+        return arr
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.vr_volume_destroy(self._h)
+            self._h = None
+
+
+def env_struct(rgb, scale=(1.0, 1.0, 1.0), rotation=None):
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    e = capi.EnvMap()
+    e.rgb = rgb.ctypes.data_as(C.POINTER(C.c_float))
+    e.height, e.width = rgb.shape[0], rgb.shape[1]
+    e.scale[:] = list(scale)
+    e.rotation[:] = list(rotation) if rotation is not None else [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    return e, rgb
+
+
+class VolumetricReSTIR:
+    """The per-frame Volumetric ReSTIR loop on one GB300."""
+
+    def __init__(self, width, height, params=None, lib=None):
+        self._lib = lib or capi.load()
+        self._opts = capi.default_options(self._lib)
+        if params:
+            self._apply(params)
+        err = C.c_int32()
+        self._h = self._lib.vr_create(C.byref(self._opts), width, height, C.byref(err))
+        if not self._h:
+            raise RuntimeError(f"vr_create failed ({err.value})")
+        self.width, self.height = width, height
+        self._keep = []
+
+    # ---- options (VolumetricReSTIRParams) ----
+    def _apply(self, params):
+        names = {k for k, _ in capi.Options._fields_}
+        for k, v in params.items():
+            if k not in names:
+                warnings.warn(f"Unknown field '{k}' in a VolumetricReSTIR dictionary")
+                continue
+            setattr(self._opts, k, v)
+
+    @property
+    def mParams(self):
+        return self._opts.as_dict()
+
+    def setParams(self, **params):
+        self._apply(params)
+        self._check(self._lib.vr_set_options(self._h, C.byref(self._opts)))
+
+    # ---- scene ----
+    def setScene(self, volume, medium, lights=(), env_rgb=None, env_scale=(1.0, 1.0, 1.0)):
+        self._volume = volume
+        self._check(self._lib.vr_set_volume(self._h, volume._h, C.byref(medium)))
+        arr = (capi.PointLight * max(1, len(lights)))(*lights) if lights else None
+        env = None
+        if env_rgb is not None:
+            env, keep = env_struct(env_rgb, env_scale)
+            self._keep = [keep]
+        self._check(self._lib.vr_set_lights(self._h, arr, len(lights), C.byref(env) if env is not None else None))
+
+    # ---- frames ----
+    def execute(self, camera, out_ptr, mvec_ptr=None, stream=0):
+        """Renders one frame into device memory (width*height float4)."""
+        self._check(self._lib.vr_render_frame(self._h, C.byref(camera), C.c_void_p(out_ptr),
+                                              C.c_void_p(mvec_ptr) if mvec_ptr else None, C.c_void_p(stream)))
+
+    def execute_host(self, camera, stream=0):
+        out = np.empty((self.height, self.width, 4), np.float32)
+        self._check(self._lib.vr_render_frame_host(self._h, C.byref(camera), out.ctypes.data_as(C.POINTER(C.c_float)),
+                                                   C.c_void_p(stream)))
+        return out
+
+    def render_reference(self, camera, accum_ptr, first_frame, num_frames, stream=0):
+        self._check(self._lib.vr_render_reference(self._h, C.byref(camera), first_frame, num_frames,
+                                                  C.c_void_p(accum_ptr), C.c_void_p(stream)))
+
+    # ---- state ----
+    def export_reservoirs(self, which=0):
+        n = self.width * self.height
+        rb = self._lib.vr_reservoir_bytes(self._h)
+        buf = np.zeros(n * rb, np.uint8)
+        self._check(self._lib.vr_export_reservoirs(self._h, which, buf.ctypes.data_as(C.c_void_p), buf.nbytes))
+        return buf
+
+    def export_extra(self, which=0):
+        n = self.width * self.height * max(self._opts.mMaxBounces - 1, 0) * 3
+        out = np.zeros(max(n, 1), np.float32)
+        self._check(self._lib.vr_export_extra_bounces(self._h, which, out.ctypes.data_as(C.POINTER(C.c_float)), out.nbytes))
+        return out[:n]
+
+    def export_features(self):
+        out = np.zeros(self.width * self.height * 2, np.int32)
+        self._check(self._lib.vr_export_features(self._h, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def export_state(self):
+        n = self._lib.vr_state_bytes(self._h)
+        buf = np.zeros(n, np.uint8)
+        self._check(self._lib.vr_export_state(self._h, buf.ctypes.data_as(C.c_void_p), buf.nbytes))
+        return buf
+
+    def import_state(self, buf):
+        buf = np.ascontiguousarray(buf, dtype=np.uint8)
+        self._check(self._lib.vr_import_state(self._h, buf.ctypes.data_as(C.c_void_p), buf.nbytes))
+
+    @property
+    def frame_count(self):
+        return self._lib.vr_frame_count(self._h)
+
+    def last_timings(self):
+        ms = (C.c_float * 16)()
+        n = C.c_int32()
+        self._lib.vr_last_timings(self._h, ms, 16, C.byref(n))
+        return list(ms[: n.value])
+
+    def kernel_time_totals(self, reset=True):
+        ms = (C.c_float * 4)()
+        n = C.c_int32()
+        self._check(self._lib.vr_kernel_time_totals(self._h, ms, 4, C.byref(n), 1 if reset else 0))
+        return list(ms[:2]), n.value
+
+    def last_launch_count(self):
+        return self._lib.vr_last_launch_count(self._h)
+
+    def _check(self, r):
+        if r != capi.VR_OK:
+            msg = self._lib.vr_last_error(self._h).decode() if getattr(self, "_h", None) else ""
+            raise RuntimeError(f"libvrestir error {r}: {msg}")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.vr_destroy(self._h)
+            self._h = None
+
+
+RESERVOIR_DTYPE_36 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
+                               ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4"),
+                               ("extraBounceStartId", "<i4")])
+RESERVOIR_DTYPE_32 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
+                               ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4")])
+
+
+def as_reservoirs(buf, max_bounces):
+    return np.frombuffer(buf.tobytes(), RESERVOIR_DTYPE_36 if max_bounces > 1 else RESERVOIR_DTYPE_32)

@@ -1,0 +1,149 @@
+"""Synthetic scenes for the workloads of this path.
+
+The reference renders GVDB (.vbx) clouds that are not available here; these procedural scenes
+stand in for them with the shapes, sizes and value ranges of the benchmark configurations:
+
+  small  : 128^3 dense fBm (4 octaves, seed 1, lacunarity 2, gain 0.5) x smooth sphere mask
+           r = 0.45 in the unit box, sigma_t 20/unit, albedo 0.9, g = 0; one point light
+           (intensity 50) at (2,2,2) + constant white environment 0.2; camera (0,0,-2.5),
+           45 deg FOV, 256x256; max path length 2, 8 candidates, temporal + 3 spatial
+           neighbours (radius 10), static camera.
+  full   : 512^3 sparse fBm (6 octaves) thresholded at 0.35 and remapped to [0,1] in 8^3
+           bricks, 4-level conservative pyramid; sigma_t 40, albedo 0.95, g = 0.6; 16 point
+           lights on a sphere of radius 3 (intensity 10) + procedural 512x256 sky; 1920x1080;
+           max path length 3, 32 candidates, temporal + 3 spatial neighbours; the camera
+           orbits 0.5 deg per frame.
+  small_fp16 : `small` with FP16 bricks.
+"""
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+
+
+@dataclass
+class SceneDesc:
+    name: str
+    width: int
+    height: int
+    volume: capi.ProceduralDesc
+    medium: capi.Medium
+    lights: list
+    env_rgb: np.ndarray            # (H, W, 3) float32 lat-long
+    env_scale: tuple = (1.0, 1.0, 1.0)
+    options: dict = field(default_factory=dict)
+    camera_radius: float = 2.5
+    camera_height: float = 0.0
+    orbit_deg_per_frame: float = 0.0
+    fov_deg: float = 45.0
+    frames: int = 16
+
+    def camera(self, frame=0):
+        ang = math.radians(self.orbit_deg_per_frame * frame)
+        pos = (-self.camera_radius * math.sin(ang), self.camera_height, -self.camera_radius * math.cos(ang))
+        c = capi.Camera()
+        c.pos[:] = [float(np.float32(v)) for v in pos]
+        c.target[:] = [0.0, 0.0, 0.0]
+        c.up[:] = [0.0, 1.0, 0.0]
+        c.fov_y = float(np.float32(math.radians(self.fov_deg)))
+        c.near_z = 0.01
+        c.far_z = 1000.0
+        return c
+
+
+def _procedural(kind, res, octaves, seed, threshold, world_min, voxel_size, fp16=False, num_mips=4,
+                base_frequency=4.0, mask_radius=0.45):
+    d = capi.ProceduralDesc()
+    d.kind = kind
+    d.res = res
+    d.num_mips = num_mips
+    d.octaves = octaves
+    d.seed = seed
+    d.lacunarity = 2.0
+    d.gain = 0.5
+    d.base_frequency = base_frequency
+    d.mask_radius = mask_radius
+    d.threshold = threshold
+    d.world_min[:] = list(world_min)
+    d.voxel_size = voxel_size
+    d.fp16 = 1 if fp16 else 0
+    return d
+
+
+def _medium(sigma_t, albedo, g):
+    m = capi.Medium()
+    ss = np.float32(sigma_t * albedo)
+    sa = np.float32(sigma_t) - ss
+    m.sigma_s[:] = [float(ss)] * 3
+    m.sigma_a[:] = [float(sa)] * 3
+    m.g = g
+    m.density_scale = 1.0
+    return m
+
+
+def constant_env(value, w=8, h=4):
+    return np.full((h, w, 3), value, dtype=np.float32)
+
+
+def sky_env(w=512, h=256):
+    """Procedural sky in lat-long layout (v = 0 at +y): zenith-to-horizon gradient, a dim
+    ground and a soft sun lobe."""
+    v = (np.arange(h, dtype=np.float64) + 0.5) / h
+    u = (np.arange(w, dtype=np.float64) + 0.5) / w
+    uu, vv = np.meshgrid(u, v)
+    theta = vv * math.pi                       # 0 at +y
+    phi = (uu - 0.5) * 2.0 * math.pi
+    d = np.stack([np.sin(theta) * np.sin(phi), np.cos(theta), -np.sin(theta) * np.cos(phi)], -1)
+    up = np.clip(d[..., 1], 0.0, 1.0)
+    zen = np.array([0.25, 0.45, 0.95])
+    hor = np.array([0.85, 0.9, 1.0])
+    sky = hor + (zen - hor) * up[..., None] ** 0.6
+    ground = np.array([0.25, 0.22, 0.2]) * np.ones_like(sky)
+    col = np.where((d[..., 1] >= 0)[..., None], sky, ground)
+    sun = np.array([0.3, 0.8, 0.5])
+    sun /= np.linalg.norm(sun)
+    lobe = np.clip(d @ sun, 0.0, 1.0) ** 256
+    col = col + lobe[..., None] * np.array([40.0, 36.0, 30.0])
+    return col.astype(np.float32)
+
+
+def sphere_lights(n, radius, intensity):
+    lights = []
+    ga = math.pi * (3.0 - math.sqrt(5.0))
+    for i in range(n):
+        y = 1.0 - 2.0 * (i + 0.5) / n
+        r = math.sqrt(max(0.0, 1.0 - y * y))
+        t = ga * i
+        l = capi.PointLight()
+        l.pos[:] = [radius * r * math.cos(t), radius * y, radius * r * math.sin(t)]
+        l.intensity[:] = [intensity] * 3
+        lights.append(l)
+    return lights
+
+
+def small(width=256, height=256, fp16=False):
+    light = capi.PointLight()
+    light.pos[:] = [2.0, 2.0, 2.0]
+    light.intensity[:] = [50.0, 50.0, 50.0]
+    return SceneDesc(
+        name="small_fp16" if fp16 else "small", width=width, height=height,
+        volume=_procedural(0, 128, 4, 1, 0.0, (-0.5, -0.5, -0.5), 1.0 / 128.0, fp16=fp16),
+        medium=_medium(20.0, 0.9, 0.0), lights=[light], env_rgb=constant_env(0.2),
+        options=dict(mMaxBounces=2, mInitialM=8, mEnableTemporalReuse=1, mEnableSpatialReuse=1, mSpatialSampleCount=4,
+                     mSampleRadius=10.0, mUseAnalyticLights=1, mUseEnvironmentLights=1),
+        camera_radius=2.5, frames=16)
+
+
+def full(width=1920, height=1080, fp16=False):
+    return SceneDesc(
+        name="full_fp16" if fp16 else "full", width=width, height=height,
+        volume=_procedural(1, 512, 6, 7, 0.35, (-1.0, -1.0, -1.0), 2.0 / 512.0, fp16=fp16, base_frequency=3.0),
+        medium=_medium(40.0, 0.95, 0.6), lights=sphere_lights(16, 3.0, 10.0), env_rgb=sky_env(),
+        options=dict(mMaxBounces=3, mInitialM=32, mEnableTemporalReuse=1, mEnableSpatialReuse=1, mSpatialSampleCount=4,
+                     mSampleRadius=10.0, mUseAnalyticLights=1, mUseEnvironmentLights=1),
+        camera_radius=2.4, camera_height=0.3, orbit_deg_per_frame=0.5, frames=64)
+
+
+CONFIGS = {"small": small, "full": full, "small_fp16": lambda **k: small(fp16=True, **k)}
