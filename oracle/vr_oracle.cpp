@@ -342,9 +342,13 @@ struct HDDA {
         mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
+    // Step (gvdbDda.slang:151-156) advances the masked axes by tDel.  The reference writes
+    // tSide += float3(mask) * tDel, whose unmasked terms are 0 * inf = NaN for a zero
+    // direction component under IEEE arithmetic and stall the walk; the select form below is
+    // the intended semantics (and what a non-IEEE-strict shader compiler produces).
     void Step() {
         t.x = t.y;
-        tSide = tSide + mk3((float)mask[0], (float)mask[1], (float)mask[2]) * tDel;
+        tSide = mk3(mask[0] ? tSide.x + tDel.x : tSide.x, mask[1] ? tSide.y + tDel.y : tSide.y, mask[2] ? tSide.z + tDel.z : tSide.z);
         p[0] += mask[0] * pStep[0]; p[1] += mask[1] * pStep[1]; p[2] += mask[2] * pStep[2];
     }
 };

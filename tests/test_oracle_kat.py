@@ -1,0 +1,108 @@
+"""Analytic known answers for the oracle's volume tracking (the reference's tests pin only the
+RNG; these pin the tracking estimators on media with closed-form answers)."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from volumetricrestirrelease_gb300 import capi
+from volumetricrestirrelease_gb300.restir import Volume
+
+SIGMA_T = 3.0
+RES = 32
+
+
+@pytest.fixture(scope="module")
+def homogeneous(vlib):
+    from oracle.oracle import Oracle
+    g = np.full((RES, RES, RES), 0.5, np.float32)
+    vol = Volume.dense(g, (-1.0, -1.0, -1.0), 2.0 / RES, num_mips=2, lib=vlib)
+    m = capi.Medium()
+    m.sigma_s[:] = [SIGMA_T * 0.8] * 3
+    m.sigma_a[:] = [SIGMA_T - SIGMA_T * 0.8] * 3
+    m.g = 0.0
+    m.density_scale = 1.0
+    o = Oracle(8, 8, capi.default_options(vlib))
+    o.set_volume(vol, m)
+    return o, vol
+
+
+def _tr(o, origin, d, tmax, method, linear=1, mip=0, seed=1, tss=1.0):
+    oa = (C.c_float * 3)(*origin)
+    da = (C.c_float * 3)(*d)
+    return o.L.vro_transmittance(o._h, oa, da, tmax, mip, linear, method, tss, seed)
+
+
+# Closed forms for a ray along +z through the centre of the homogeneous box (32 voxels of
+# density 0.5, sigma_t 3, voxel 1/16): point-sampled analytic tracking and midpoint ray
+# marching integrate 32 voxels exactly (tau = 3); trilinear analytic tracking walks
+# vertex-centred cells and starts at the first cell at or above index 0, skipping the
+# half voxel [0, 0.5) where the trilinear field ramps from 0.25 to 0.5 (tau = 3*15.6875/16);
+# the (residual) ratio trackers estimate the transmittance of the full trilinear field
+# (tau = 3*15.875/16).
+TAU_POINT = SIGMA_T * 0.5 * 2.0
+TAU_TRI_ANALYTIC = SIGMA_T * 15.6875 * (2.0 / RES)
+TAU_TRI = SIGMA_T * 15.875 * (2.0 / RES)
+
+
+@pytest.mark.parametrize("direction", [(0.0, 0.0, 1.0), (0.03, -0.02, 1.0)])
+def test_point_sampled_analytic_tracking(homogeneous, direction):
+    o, _ = homogeneous
+    d = np.array(direction, np.float64)
+    d /= np.linalg.norm(d)
+    t = _tr(o, (0.013, -0.021, -3.0), tuple(d), 1e30, capi.VR_TRACK_ANALYTIC, linear=0)
+    chord = 2.0 / d[2]
+    assert t == pytest.approx(math.exp(-SIGMA_T * 0.5 * chord), rel=2e-5)
+
+
+def test_segment_ending_inside(homogeneous):
+    o, _ = homogeneous
+    t = _tr(o, (0.013, -0.021, -3.0), (0.0, 0.0, 1.0), 3.3, capi.VR_TRACK_ANALYTIC, linear=0)
+    assert t == pytest.approx(math.exp(-SIGMA_T * 0.5 * 1.3), rel=2e-5)
+
+
+def test_ray_marching_midpoint(homogeneous):
+    o, _ = homogeneous
+    for lin in (0, 1):
+        t = _tr(o, (0.013, -0.021, -3.0), (0.0, 0.0, 1.0), 1e30, capi.VR_TRACK_RAY_MARCHING, linear=lin)
+        assert t == pytest.approx(math.exp(-TAU_POINT), rel=2e-5)
+
+
+def test_trilinear_analytic_tracking(homogeneous):
+    o, _ = homogeneous
+    t = _tr(o, (0.013, -0.021, -3.0), (0.0, 0.0, 1.0), 1e30, capi.VR_TRACK_ANALYTIC, linear=1)
+    assert t == pytest.approx(math.exp(-TAU_TRI_ANALYTIC), rel=2e-5)
+
+
+@pytest.mark.parametrize("method", [capi.VR_TRACK_RATIO, capi.VR_TRACK_RESIDUAL_RATIO, capi.VR_TRACK_ANALOG_RESIDUAL_RATIO])
+def test_ratio_trackers_unbiased(homogeneous, method):
+    o, _ = homogeneous
+    vals = np.array([_tr(o, (0.1, 0.2, -3.0), (0.0, 0.0, 1.0), 1e30, method, seed=s) for s in range(3000)])
+    expect = math.exp(-TAU_TRI)
+    assert abs(vals.mean() - expect) < 4 * vals.std() / math.sqrt(len(vals)) + 1e-4
+
+
+def test_distance_sampling_mean_free_path(homogeneous):
+    o, _ = homogeneous
+    sig = SIGMA_T * 0.5
+    hits = []
+    for s in range(2000):
+        out = (C.c_float * 3)()
+        o.L.vro_sample_distance(o._h, (C.c_float * 3)(0.05, 0.07, -3.0), (C.c_float * 3)(0, 0, 1), 0, 0, s, out)
+        hits.append(out[0])
+    hits = np.array(hits)
+    inside = hits[hits < 1e30] - 2.0            # the box starts at distance 2
+    frac_escape = np.mean(hits >= 1e30)
+    assert abs(frac_escape - math.exp(-sig * 2.0)) < 0.03
+    # truncated exponential mean on [0, 2]
+    mean_trunc = 1 / sig - 2.0 * math.exp(-2 * sig) / (1 - math.exp(-2 * sig))
+    assert abs(inside.mean() - mean_trunc) < 0.05
+
+
+def test_density_lookup_trilinear(homogeneous):
+    o, _ = homogeneous
+    p = (C.c_float * 3)(0.3, -0.2, 0.1)
+    assert o.L.vro_density_world(o._h, p, 0) == pytest.approx(0.5, abs=1e-7)
+    p = (C.c_float * 3)(5.0, 0.0, 0.0)
+    assert o.L.vro_density_world(o._h, p, 0) == 0.0

@@ -304,9 +304,10 @@ struct HDDA {
         mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
+    // advances only the masked axes (a zero direction component has tDel = inf)
     __device__ __forceinline__ void step() {
         t.x = t.y;
-        tSide = tSide + mk3((float)mask[0], (float)mask[1], (float)mask[2]) * tDel;
+        tSide = mk3(mask[0] ? tSide.x + tDel.x : tSide.x, mask[1] ? tSide.y + tDel.y : tSide.y, mask[2] ? tSide.z + tDel.z : tSide.z);
         p[0] += mask[0] * ps[0]; p[1] += mask[1] * ps[1]; p[2] += mask[2] * ps[2];
     }
 };
