@@ -21,7 +21,7 @@ LIB = PKG / "_lib" / "libvrestir.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-v"]
-HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h"]
+HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h", "vr_noalloc.h"]
 
 
 def _nvcc():
@@ -56,6 +56,9 @@ def build(force=False, jobs=None):
         obj = BUILD / f"frame_kernels_mb{mb}.o"
         src = CSRC / "frame_kernels.cu"
         units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-c", str(src), "-o", str(obj)]))
+    obj = BUILD / "noalloc.o"
+    src = CSRC / "noalloc.cu"
+    units.append((obj, [src, CSRC / "vr_noalloc.h"] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))
     obj = BUILD / "context.o"
     src = CSRC / "context.cu"
     units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))

@@ -109,6 +109,7 @@ SIGNATURES = {
     "vr_render_frame": (_i32, [_P, C.POINTER(Camera), _P, _P, _P]),
     "vr_render_frame_host": (_i32, [_P, C.POINTER(Camera), C.POINTER(_f32), _P]),
     "vr_render_reference": (_i32, [_P, C.POINTER(Camera), _i32, _i32, _P, _P]),
+    "vr_render_frame_noalloc": (_i32, [_P, C.POINTER(Camera), _i32, _P, _P]),
     "vr_reservoir_bytes": (_i32, [_P]),
     "vr_export_reservoirs": (_i32, [_P, _i32, _P, C.c_size_t]),
     "vr_export_extra_bounces": (_i32, [_P, _i32, C.POINTER(_f32), C.c_size_t]),

@@ -1033,3 +1033,55 @@ extern "C" int vr_import_state(vr_context* c, const void* host, size_t bytes) {
     c->prev = h.prev;
     return check_cuda(c, "import state");
 }
+
+// ---------------------------------------------------------------------------------------
+// support for the allocation-free frame entry point (noalloc.cu): validation and launch
+// parameters from a context, without touching its buffers, counters or history
+// ---------------------------------------------------------------------------------------
+#include "vr_noalloc.h"
+namespace vrk {
+int noalloc_prepare(vr_context* c, const vr_camera* cam, int32_t frame_index, NoAllocFrame* f) {
+    if (!cam || !f) { c->err = "null camera or frame"; return VR_ERR_INVALID_ARG; }
+    if (!c->hasVolume) { c->err = "no volume bound (vr_set_volume)"; return VR_ERR_STATE; }
+    const vr_options& o = c->opts;
+    if (o.mEnableTemporalReuse || o.mUseReference) {
+        c->err = "vr_render_frame_noalloc renders frames without history: disable mEnableTemporalReuse and mUseReference";
+        return VR_ERR_INVALID_ARG;
+    }
+    if (o.mMaxBounces > kNoAllocMaxBounces) { c->err = "vr_render_frame_noalloc supports mMaxBounces <= 2"; return VR_ERR_INVALID_ARG; }
+    if ((int64_t)c->W * c->H > kNoAllocMaxPixels) {
+        c->err = "vr_render_frame_noalloc supports at most 65536 pixels (e.g. 256x256); its scratch is a fixed static buffer";
+        return VR_ERR_INVALID_ARG;
+    }
+    if (frame_index < 0) { c->err = "frame_index must be >= 0"; return VR_ERR_INVALID_ARG; }
+    std::string why;
+    if (!slots_present(c, why)) { c->err = why; return VR_ERR_INVALID_ARG; }
+    if (o.mUseAnalyticLights && c->scene.numLights == 0) { c->err = "mUseAnalyticLights needs at least one point light"; return VR_ERR_INVALID_ARG; }
+    if (o.mUseEnvironmentLights && !c->scene.hasEnv) { c->err = "mUseEnvironmentLights needs an environment map"; return VR_ERR_INVALID_ARG; }
+    CamFrame cf = camera_frame(*cam, c->W, c->H);
+    int numTotalRounds = (o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0) + 0 + 1 + 1;
+    f->P = frame_params(c, cf, numTotalRounds);
+    f->P.frameCount = frame_index;
+    f->P.isFirstFrame = 1;
+    f->P.temporalEnabled = 0;
+    f->scene = &c->scene;
+    f->W = c->W; f->H = c->H;
+    f->maxBounces = o.mMaxBounces;
+    f->spatial = o.mEnableSpatialReuse;
+    f->rounds = o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0;
+    for (int r = 0; r < f->rounds; ++r) {
+        vrd::SpatialParams& S = f->S[r];
+        memset(&S, 0, sizeof(S));
+        S.in = r % 2;
+        S.out = (r + 1) % 2;
+        S.roundId = r;
+        S.numRounds = o.mSpatialReuseRounds + 1 + 1;
+        S.rid = r + 1;
+        S.last = r == o.mSpatialReuseRounds - 1;
+        S.writeHistory = 0;
+        neighbor_offsets(o, ((o.mSpatialReuseRounds + 1) * frame_index + r) % 16, S.offs);
+    }
+    return VR_OK;
+}
+void noalloc_error(vr_context* c, const char* msg) { c->err = msg; }
+}  // namespace vrk
