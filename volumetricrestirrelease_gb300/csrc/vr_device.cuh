@@ -236,20 +236,57 @@ __device__ __forceinline__ float trilinear(const DevSlot& s, int brick, f3 p) {
     float y0 = lerp_(x00, x10, fy), y1 = lerp_(x01, x11, fy);
     return lerp_(y0, y1, fz);
 }
+// Unclamped accessors for positions the caller's loop guard keeps inside the brick
+// (p in [0, 8]^3 for trilinear, cell in [0, 7]^3 for point and 8-corner fetches): one base
+// offset and seven constant displacements into the 10^3 brick.
+__device__ __forceinline__ void cornerValues(const DevSlot& s, size_t base, float c[8]) {
+    if (s.f32) {
+        const float* d = s.f32 + base;
+        c[0] = __ldg(d); c[1] = __ldg(d + 1); c[2] = __ldg(d + 10); c[3] = __ldg(d + 11);
+        c[4] = __ldg(d + 100); c[5] = __ldg(d + 101); c[6] = __ldg(d + 110); c[7] = __ldg(d + 111);
+    } else {
+        const __half* d = s.f16 + base;
+        c[0] = __half2float(__ldg(d)); c[1] = __half2float(__ldg(d + 1));
+        c[2] = __half2float(__ldg(d + 10)); c[3] = __half2float(__ldg(d + 11));
+        c[4] = __half2float(__ldg(d + 100)); c[5] = __half2float(__ldg(d + 101));
+        c[6] = __half2float(__ldg(d + 110)); c[7] = __half2float(__ldg(d + 111));
+    }
+}
+__device__ __forceinline__ float trilinearIn(const DevSlot& s, int brick, f3 p) {
+    float qx = p.x - 0.5f, qy = p.y - 0.5f, qz = p.z - 0.5f;
+    float fx0 = vr::floor_(qx), fy0 = vr::floor_(qy), fz0 = vr::floor_(qz);
+    int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    float fx = qx - fx0, fy = qy - fy0, fz = qz - fz0;
+    float c[8];
+    cornerValues(s, (size_t)brick * 1000 + (size_t)(((iz + 1) * 10 + (iy + 1)) * 10 + (ix + 1)), c);
+    float x00 = lerp_(c[0], c[1], fx), x10 = lerp_(c[2], c[3], fx);
+    float x01 = lerp_(c[4], c[5], fx), x11 = lerp_(c[6], c[7], fx);
+    float y0 = lerp_(x00, x10, fy), y1 = lerp_(x01, x11, fy);
+    return lerp_(y0, y1, fz);
+}
+__device__ __forceinline__ float voxelIn(const DevSlot& s, int brick, int x, int y, int z) {
+    size_t o = (size_t)brick * 1000 + (size_t)(((z + 1) * 10 + (y + 1)) * 10 + (x + 1));
+    return s.f32 ? __ldg(&s.f32[o]) : __half2float(__ldg(&s.f16[o]));
+}
+// density at a brick-local position inside the brick (loop-guarded callers)
 __device__ __forceinline__ float densityLocal(int mip, int brick, f3 p, bool linear) {
     const DevSlot& s = c_scene.slots[mip];
-    float v = linear ? trilinear(s, brick, p)
-                     : voxel(s, brick, vr::f2i(vr::floor_(p.x)), vr::f2i(vr::floor_(p.y)), vr::f2i(vr::floor_(p.z)));
+    float v = linear ? trilinearIn(s, brick, p) : voxelIn(s, brick, (int)vr::floor_(p.x), (int)vr::floor_(p.y), (int)vr::floor_(p.z));
     return v * 1.0f * c_scene.dscale;
 }
+// density at a position that may sit a rounding error outside the brick (delta and ratio
+// tracking sample free-flight positions): clamped indices
+__device__ __forceinline__ float densityLocalClamped(int mip, int brick, f3 p) {
+    return trilinear(c_scene.slots[mip], brick, p) * 1.0f * c_scene.dscale;
+}
 __device__ __forceinline__ float densityCell(int mip, int brick, const int p[3]) {
-    return voxel(c_scene.slots[mip], brick, p[0], p[1], p[2]) * 1.0f * c_scene.dscale;
+    return voxelIn(c_scene.slots[mip], brick, p[0], p[1], p[2]) * 1.0f * c_scene.dscale;
 }
 __device__ __forceinline__ void fetchEightSigma(int mip, int brick, const int p[3], float v[8]) {
     const DevSlot& s = c_scene.slots[mip];
+    cornerValues(s, (size_t)brick * 1000 + (size_t)(((p[2] + 1) * 10 + (p[1] + 1)) * 10 + (p[0] + 1)), v);
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
-        v[i] = voxel(s, brick, p[0] + (i % 2), p[1] + (i % 4) / 2, p[2] + i / 4) * 1.0f * c_scene.dscale * c_scene.sigma_t;
+    for (int i = 0; i < 8; ++i) v[i] = v[i] * 1.0f * c_scene.dscale * c_scene.sigma_t;
 }
 __device__ inline int findBrick(const DevSlot& s, f3 pos, f3& vmin) {
     if (pos.x < 0.f || pos.y < 0.f || pos.z < 0.f || pos.x >= 4096.f || pos.y >= 4096.f || pos.z >= 4096.f) return -1;
@@ -271,7 +308,7 @@ static __device__ __noinline__ float densityWorld(f3 pw, int mip) {
     f3 vmin;
     int br = findBrick(s, p, vmin);
     if (br < 0) return 0.f;
-    return trilinear(s, br, p - vmin) * c_scene.dscale;
+    return trilinearIn(s, br, p - vmin) * c_scene.dscale;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -470,12 +507,28 @@ struct TrRayMarch {
         f3 wp = ray.o + t * ray.d;
         f3 p = wp - vl;
         const f3 wpt = mult * tStep * ray.d;
-        for (int iter = 0; iter < kMaxBrickSteps && inLeafF(p); iter++) {
+        // Two samples per trip: the second sample's position and the exit tests are computed
+        // exactly as the next iteration would, so both loads are in flight together while the
+        // optical depth is still summed sample by sample.
+        int iter = 0;
+        while (iter < kMaxBrickSteps && inLeafF(p)) {
             if (t >= tFar) { Tr = vr::exp_(Tr); return true; }
-            float sigma_t = densityLocal(mip, brick, p, lin) * c_scene.sigma_t;
+            const f3 p1 = p + wpt;
+            const float t1 = t + mult * tStep;
+            const bool second = iter + 1 < kMaxBrickSteps && inLeafF(p1) && !(t1 >= tFar);
+            float d0 = densityLocal(mip, brick, p, lin);
+            float d1 = second ? densityLocal(mip, brick, p1, lin) : 0.f;
+            float sigma_t = d0 * c_scene.sigma_t;
             Tr += -sigma_t * (iter == 0 ? 1.f : mult) * tStep;
+            p = p1;
+            t = t1;
+            iter++;
+            if (!second) continue;
+            sigma_t = d1 * c_scene.sigma_t;
+            Tr += -sigma_t * mult * tStep;
             p = p + wpt;
             t += mult * tStep;
+            iter++;
         }
         return false;
     }
@@ -632,7 +685,7 @@ struct DeltaTrack {
                 t -= vr::log_(1 - vr::next1D(sg)) * invMax / c_scene.sigma_t;
                 if (t >= tc || t >= curTMax) break;
                 f3 p = (ray.o + t * ray.d) - vl;
-                float density = densityLocal(mip, brick, p, true);
+                float density = densityLocalClamped(mip, brick, p);
                 if ((density - minD) * invMax > vr::next1D(sg)) { setMi(t); return true; }
             }
             t = vr::fmin_(tc, t);
@@ -675,7 +728,7 @@ struct ResidualRatio {
                 t -= vr::log_(1 - vr::next1D(sg)) * inv;
                 if (t >= curTMax) break;
                 f3 p = (ray.o + t * ray.d) - vl;
-                float mu = densityLocal(mip, brick, p, true) * st;
+                float mu = densityLocalClamped(mip, brick, p) * st;
                 T_r *= 1 - (mu - mu_c) * inv;
             }
         }

@@ -320,8 +320,16 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
 // ---------------------------------------------------------------------------------------
 // k_initial: GenerateFeatures + TraceRays (+ TemporalReuse)
 // ---------------------------------------------------------------------------------------
+// Register budget: 5 blocks of 128 threads per SM (<= 102 registers per thread).  Measured on
+// the full workload against 1, 4 and 6 blocks; the extra residency outweighs the added spills.
+#ifndef VR_KINIT_MIN_BLOCKS
+#define VR_KINIT_MIN_BLOCKS 5
+#endif
+#ifndef VR_KSPAT_MIN_BLOCKS
+#define VR_KSPAT_MIN_BLOCKS 5
+#endif
 template <int MB>
-__global__ void __launch_bounds__(128) k_initial(const FrameParams P, const FrameBuffers B) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const FrameParams P, const FrameBuffers B) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -426,7 +434,7 @@ struct SpatialParams {
 };
 
 template <int MB>
-__global__ void __launch_bounds__(128) k_spatial(const FrameParams P, const FrameBuffers B, const SpatialParams S) {
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const FrameParams P, const FrameBuffers B, const SpatialParams S) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
