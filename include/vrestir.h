@@ -290,6 +290,10 @@ int vr_last_transfer_bytes(const vr_context* ctx, int64_t* h2d, int64_t* d2h);
  *      can check device/host bit equality.  op: 0 exp, 1 log, 2 sin, 3 cos, 4 atan2, 5 acos,
  *      6 pow, 7 sqrt.  In/out are host arrays of n floats. ---- */
 int vr_selftest_math(int32_t op, const float* a, const float* b, float* out, int32_t n);
+/* One 128x64x64 BF16 tensor-core product (tcgen05, FP32 accumulation in TMEM):
+ * D[128x64] = A[128x64] * B[64x64]^T, row-major bf16 inputs, host arrays.  variant 0/1 selects
+ * the descriptor stride convention under test. */
+int vr_selftest_umma(const uint16_t* A, const uint16_t* B, float* D, int32_t variant);
 /* For n pixel cases (px, py, sampleNumber) returns the first `draws` values of sampleNext1D. */
 int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out);
 

@@ -56,6 +56,9 @@ def build(force=False, jobs=None):
         obj = BUILD / f"frame_kernels_mb{mb}.o"
         src = CSRC / "frame_kernels.cu"
         units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-c", str(src), "-o", str(obj)]))
+    obj = BUILD / "lp.o"
+    src = CSRC / "lp.cu"
+    units.append((obj, [src, CSRC / "umma.cuh"] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))
     obj = BUILD / "noalloc.o"
     src = CSRC / "noalloc.cu"
     units.append((obj, [src, CSRC / "vr_noalloc.h"] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))

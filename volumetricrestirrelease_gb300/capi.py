@@ -124,6 +124,7 @@ SIGNATURES = {
     "vr_last_transfer_bytes": (_i32, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "vr_selftest_math": (_i32, [_i32, C.POINTER(_f32), C.POINTER(_f32), C.POINTER(_f32), _i32]),
     "vr_selftest_rng": (_i32, [C.POINTER(_u32), _i32, _i32, C.POINTER(_f32)]),
+    "vr_selftest_umma": (_i32, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(_f32), _i32]),
 }
 
 _LIB = None
