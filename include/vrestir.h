@@ -105,6 +105,18 @@ typedef struct vr_options {
     uint32_t mFinalVisibilityTrackingMethod;    /* VR_TRACK_ANALYTIC */
     uint32_t mFinalLightTrackingMethod;         /* VR_TRACK_ANALYTIC */
     float mFinalTStepScale;                     /* 0.2 */
+    /* Learned target function for the initial candidates (no counterpart in the reference):
+     * a transmittance MLP replaces the marched light visibility inside the initial RIS target
+     * (ComputeInitialSample.slang's SampleDirectLighting shadow ray).  The marched estimators
+     * keep evaluating every later p_hat (TraceRays.cs.slang:176-183, temporal, spatial) and the
+     * final shading, so the estimator stays unbiased for any network.  Needs temporal or
+     * spatial reuse. */
+    int32_t mUseLearnedPHat;                    /* 0 */
+    int32_t mLearnedTrainSamples;               /* 1048576 new training samples per frame (0: frozen) */
+    int32_t mLearnedBatch;                      /* 16384 samples per Adam step */
+    float mLearnedLearningRate;                 /* 1e-3 */
+    float mLearnedTFloor;                       /* 0.02: lower clamp of the predicted transmittance */
+    uint32_t mLearnedSeed;                      /* 1: weight initialisation and training streams */
 } vr_options;
 
 /* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */
@@ -285,6 +297,34 @@ int32_t vr_last_launch_count(const vr_context* ctx);
 /* Host->device and device->host bytes moved by the last frame call (scene constants and
  * launch parameters in; the image out for vr_render_frame_host). */
 int vr_last_transfer_bytes(const vr_context* ctx, int64_t* h2d, int64_t* d2h);
+
+/* ---- learned target: the transmittance network (no counterpart in the reference) ----
+ * Parameters: VR_NET_PARAMS FP32 values, per hidden layer l = 0..3 a [64 out][64 in] weight
+ * matrix (layer 0: 60 encoded inputs, 4 zero pads) then 64 biases; then 64 output weights and
+ * the output bias.  Inference uses BF16 weights and activations with FP32 accumulation.
+ * Queries and samples are records of 8 floats: x, y, z, wx, wy, wz, tmax, target (training) or
+ * slot (the frame's own query list).  Positions are normalised to the bound volume's box. */
+#define VR_NET_PARAMS 16705
+int vr_net_get_params(vr_context* ctx, float* host_params);
+/* Replaces the weights and resets the Adam moments and step counter. */
+int vr_net_set_params(vr_context* ctx, const float* host_params);
+/* T(x, w) = clamp(exp(net(x, w)), mLearnedTFloor, 1) for n device query records into
+ * out_device (n floats), on the tensor cores. */
+int vr_net_infer(vr_context* ctx, const float* queries_device, int32_t n, float* out_device, void* stream);
+/* Mean squared error of T against the targets of n device samples and its gradient
+ * (VR_NET_PARAMS floats, host), without changing the weights.  Synchronises. */
+int vr_net_gradients(vr_context* ctx, const float* samples_device, int32_t n, float* grads_host, float* loss_host);
+/* One Adam step (mLearnedLearningRate, beta 0.9 / 0.999, eps 1e-8) on n device samples. */
+int vr_net_train_step(vr_context* ctx, const float* samples_device, int32_t n, float* loss_host);
+/* Buffers of the last learned-target frame, copied to host memory:
+ * which 0: T per vertex slot, mInitialM * mMaxBounces * width * height floats (slot
+ *          (c * mMaxBounces + b) * width * height + pixel; defined where a query was made);
+ * which 1: the query list, query_count records of 8 floats (in arbitrary order);
+ * which 2: the training samples of the frame, mLearnedTrainSamples records of 8 floats
+ *          (tmax < 0 marks a sample whose path left the volume);
+ * which 3: the loss of each Adam step of the frame (floats).
+ * *count receives the number of records (or floats for 0 and 3). */
+int vr_export_learned(vr_context* ctx, int32_t which, void* host, size_t bytes, int64_t* count);
 
 /* ---- self tests: elementary functions and the RNG evaluated by a device kernel, so callers
  *      can check device/host bit equality.  op: 0 exp, 1 log, 2 sin, 3 cos, 4 atan2, 5 acos,

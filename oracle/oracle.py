@@ -38,6 +38,11 @@ def _load():
         "vro_rng": (None, [P, C.c_int, C.c_int, P]),
         "vro_xoshiro": (None, [P, C.c_int, P]),
         "vro_splitmix": (None, [C.c_uint64, C.c_int, P]),
+        "vro_set_net": (None, [P, P, P, P]),
+        "vro_set_lp_T": (None, [P, P, C.c_int64]),
+        "vro_export_lp": (C.c_int64, [P, C.c_int, P, C.c_int64]),
+        "vro_net_forward": (None, [P, P, P, C.c_float, P, C.c_int, P]),
+        "vro_net_gradients": (None, [P, P, P, P, C.c_int, P, P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -110,6 +115,27 @@ class Oracle:
             raise RuntimeError(f"oracle reference status {r}")
         return accum
 
+    # ---- learned target ----
+    def set_net(self, params, box):
+        """params: VR_NET_PARAMS float32; box: (bmin[3], binv[3])."""
+        self._net = np.ascontiguousarray(params, np.float32)
+        self._box = [np.ascontiguousarray(b, np.float32) for b in box]
+        self.L.vro_set_net(self._h, _ptr(self._net), _ptr(self._box[0]), _ptr(self._box[1]))
+
+    def set_lp_T(self, T=None):
+        """Per-slot transmittance to use instead of the CPU network (None: use the network)."""
+        if T is None:
+            self.L.vro_set_lp_T(self._h, None, 0)
+        else:
+            self._T = np.ascontiguousarray(T, np.float32)
+            self.L.vro_set_lp_T(self._h, _ptr(self._T), self._T.size)
+
+    def export_lp(self, which):
+        n = self.L.vro_export_lp(self._h, which, None, 0)
+        out = np.zeros(n, np.float32)
+        self.L.vro_export_lp(self._h, which, _ptr(out), n)
+        return out.reshape(-1, 8) if which in (0, 2) else out
+
     def export_reservoirs(self, which=0):
         from volumetricrestirrelease_gb300.restir import RESERVOIR_DTYPE_36
         out = np.zeros(self.width * self.height, RESERVOIR_DTYPE_36)
@@ -163,3 +189,24 @@ def rng(cases, draws):
     out = np.zeros((len(cases), draws), np.float32)
     lib().vro_rng(_ptr(cases), len(cases), draws, _ptr(out))
     return out
+
+
+def net_forward(params, box, floor, queries):
+    """CPU network: T for (n, 8) query records (index-order FP32 accumulation)."""
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 8)
+    P = np.ascontiguousarray(params, np.float32)
+    b0, b1 = [np.ascontiguousarray(b, np.float32) for b in box]
+    out = np.zeros(len(q), np.float32)
+    lib().vro_net_forward(_ptr(P), _ptr(b0), _ptr(b1), float(floor), _ptr(q), len(q), _ptr(out))
+    return out
+
+
+def net_gradients(params, box, samples):
+    """Loss and gradient of the training step, summed in the training kernel's order."""
+    s = np.ascontiguousarray(samples, np.float32).reshape(-1, 8)
+    P = np.ascontiguousarray(params, np.float32)
+    b0, b1 = [np.ascontiguousarray(b, np.float32) for b in box]
+    g = np.zeros(len(P), np.float32)
+    loss = np.zeros(1, np.float32)
+    lib().vro_net_gradients(_ptr(P), _ptr(b0), _ptr(b1), _ptr(s), len(s), _ptr(g), _ptr(loss))
+    return float(loss[0]), g

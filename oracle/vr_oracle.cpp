@@ -80,6 +80,16 @@ static bool simpleResampleStep(const Reservoir& reservoir, Reservoir& state, Rng
     if (selectSample) copySample(reservoir, state);
     return selectSample;
 }
+// simpleResampleStep with its uniform drawn beforehand (the learned-target pass)
+static bool simpleResampleStepU(const Reservoir& reservoir, Reservoir& state, float u) {
+    float w = reservoir.runningSum;
+    state.M += reservoir.M;
+    if (w <= 0.0f) return false;
+    state.runningSum += w;
+    bool sel = u * state.runningSum < w;
+    if (sel) copySample(reservoir, state);
+    return sel;
+}
 // Reservoir.slang:59-87
 static bool simpleResampleStepWithMaxM(const Reservoir& reservoir, float MThreshold, Reservoir& state, Rng& sg) {
     float correctedM = fmin_(MThreshold, reservoir.M);
@@ -1181,6 +1191,288 @@ static Reservoir ComputeInitialSample(Ctx& c, Ray primaryRay, float preHit, floa
 }
 
 // ---------------------------------------------------------------------------------------
+// Learned target (no counterpart in the reference): the product's definition restated.
+// A transmittance MLP T(x, w) replaces the marched light visibility of the initial RIS target.
+// Network: 5 query scalars (x normalised to the volume box, theta/pi, phi/2pi + 1/2), each
+// encoded as sin/cos of 2^k pi s (k < 6, higher bands by the double-angle recurrences) -> 60
+// features + 4 zero pads; 4 hidden ReLU layers of 64; T = clamp(exp(o), floor, 1).  Weights
+// and activations are rounded to BF16, products accumulated in FP32 in index order.
+// ---------------------------------------------------------------------------------------
+namespace lpo {
+const int kIn = 60, kInPad = 64, kHid = 64, kLayers = 4, kLayerStride = 64 * 64 + 64;
+const int kOutW = kLayers * kLayerStride, kOutB = kOutW + 64, kParams = kOutB + 1;
+
+static uint16_t toBf(float f) {
+    uint32_t u = f2u(f);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    return (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);
+}
+static float fromBf(uint16_t b) { return u2f((uint32_t)b << 16); }
+static float rb(float f) { return fromBf(toBf(f)); }
+
+static void features(const float x[3], const float w[3], const float bmin[3], const float binv[3], float f[kInPad]) {
+    float s[5];
+    for (int i = 0; i < 3; ++i) s[i] = (x[i] - bmin[i]) * binv[i];
+    float wy = w[1] > 1.f ? 1.f : (w[1] < -1.f ? -1.f : w[1]);
+    s[3] = acos_(wy) * kM_1_PI;
+    s[4] = atan2_(w[2], w[0]) * kM_1_2PI + 0.5f;
+    for (int i = 0; i < 5; ++i) {
+        float a = s[i] * kM_PI;
+        float sn = sin_(a), cs = cos_(a);
+        for (int k = 0; k < 6; ++k) {
+            f[12 * i + 2 * k] = sn;
+            f[12 * i + 2 * k + 1] = cs;
+            float s2 = 2.f * sn * cs, c2 = cs * cs - sn * sn;
+            sn = s2; cs = c2;
+        }
+    }
+    for (int k = kIn; k < kInPad; ++k) f[k] = 0.f;
+}
+
+// forward pass keeping the BF16 activations of every layer (act[0] = encoded input)
+static float forward(const float* P, const float x[3], const float w[3], const float bmin[3], const float binv[3], float act[5][64]) {
+    float f[kInPad];
+    features(x, w, bmin, binv, f);
+    for (int k = 0; k < kInPad; ++k) act[0][k] = rb(f[k]);
+    for (int l = 0; l < kLayers; ++l) {
+        const float* W = P + l * kLayerStride;
+        for (int n = 0; n < kHid; ++n) {
+            float acc = 0.f;
+            for (int k = 0; k < kInPad; ++k) acc += rb(W[n * 64 + k]) * act[l][k];
+            float a = acc + W[4096 + n];
+            act[l + 1][n] = rb(a > 0.f ? a : 0.f);
+        }
+    }
+    float o = 0.f;
+    for (int k = 0; k < kHid; ++k) o += act[4][k] * rb(P[kOutW + k]);
+    return o + P[kOutB];
+}
+static float predict(float o, float floor_) {
+    float t = exp_(o);
+    t = t < floor_ ? floor_ : t;
+    return t > 1.f ? 1.f : t;
+}
+
+// gradient of mean((exp(o) - target)^2) in the training kernel's order: per chunk of 128
+// samples the sums run over the samples in order, then the chunk sums in chunk order
+static void gradients(const float* P, const float* samples, int n, const float bmin[3], const float binv[3], float* grad, float* loss) {
+    const float invB = 1.f / (float)n;
+    std::vector<float> tot(kParams, 0.f), part(kParams);
+    float lossTot = 0.f;
+    std::vector<float> act((size_t)128 * 5 * 64), g(128), lv(128), dzs((size_t)128 * 64), dhs((size_t)128 * 64);
+    for (int c0 = 0; c0 < n; c0 += 128) {
+        std::fill(part.begin(), part.end(), 0.f);
+        for (int t = 0; t < 128; ++t) {
+            const int si = c0 + t;
+            float (*a)[64] = reinterpret_cast<float (*)[64]>(&act[(size_t)t * 320]);
+            g[t] = 0.f; lv[t] = 0.f;
+            bool valid = si < n;
+            float x[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+            if (valid) {
+                const float* q = samples + (size_t)si * 8;
+                x[0] = q[0]; x[1] = q[1]; x[2] = q[2]; w[0] = q[3]; w[1] = q[4]; w[2] = q[5];
+                valid = q[6] >= 0.f;
+            }
+            float o;
+            if (si < n) o = forward(P, x, w, bmin, binv, a);
+            else {
+                for (int k = 0; k < 64; ++k) a[0][k] = 0.f;
+                for (int l = 0; l < kLayers; ++l)
+                    for (int m = 0; m < kHid; ++m) {
+                        float acc = 0.f;
+                        for (int k = 0; k < kInPad; ++k) acc += rb(P[l * kLayerStride + m * 64 + k]) * a[l][k];
+                        float z = acc + P[l * kLayerStride + 4096 + m];
+                        a[l + 1][m] = rb(z > 0.f ? z : 0.f);
+                    }
+                o = 0.f;
+                for (int k = 0; k < kHid; ++k) o += a[4][k] * rb(P[kOutW + k]);
+                o += P[kOutB];
+            }
+            (void)o;
+            if (valid) {
+                float p = exp_(o);
+                float d = p - samples[(size_t)si * 8 + 7];
+                g[t] = 2.f * d * p * invB;
+                lv[t] = d * d * invB;
+            }
+            for (int k = 0; k < kHid; ++k) dhs[(size_t)t * 64 + k] = g[t] * rb(P[kOutW + k]);
+        }
+        for (int k = 0; k < kHid; ++k) {
+            float acc = 0.f;
+            for (int t = 0; t < 128; ++t) acc += g[t] * act[(size_t)t * 320 + 4 * 64 + k];
+            part[kOutW + k] = acc;
+        }
+        {
+            float acc = 0.f, ls = 0.f;
+            for (int t = 0; t < 128; ++t) { acc += g[t]; ls += lv[t]; }
+            part[kOutB] = acc;
+            lossTot += ls;
+        }
+        for (int l = kLayers - 1; l >= 0; --l) {
+            const float* W = P + l * kLayerStride;
+            for (int t = 0; t < 128; ++t) {
+                float* dz = &dzs[(size_t)t * 64];
+                float* dh = &dhs[(size_t)t * 64];
+                for (int m = 0; m < kHid; ++m) dz[m] = act[(size_t)t * 320 + (l + 1) * 64 + m] > 0.f ? dh[m] : 0.f;
+                if (l > 0)
+                    for (int k = 0; k < kHid; ++k) {
+                        float acc = 0.f;
+                        for (int m = 0; m < kHid; ++m) acc += rb(W[m * 64 + k]) * dz[m];
+                        dh[k] = acc;
+                    }
+            }
+            for (int m = 0; m < kHid; ++m) {
+                float accb = 0.f;
+                float acc[64];
+                for (int k = 0; k < 64; ++k) acc[k] = 0.f;
+                for (int t = 0; t < 128; ++t) {
+                    float d = dzs[(size_t)t * 64 + m];
+                    accb += d;
+                    for (int k = 0; k < 64; ++k) acc[k] += d * act[(size_t)t * 320 + l * 64 + k];
+                }
+                for (int k = 0; k < 64; ++k) part[l * kLayerStride + m * 64 + k] = acc[k];
+                part[l * kLayerStride + 4096 + m] = accb;
+            }
+        }
+        for (int i = 0; i < kParams; ++i) tot[i] += part[i];
+    }
+    for (int i = 0; i < kParams; ++i) grad[i] = tot[i];
+    *loss = lossTot;
+}
+}  // namespace lpo
+
+// vertex record of the split initial pass (see ComputeInitialSampleLP)
+struct LpVertex { float a, b, uv0, uv1; int lightID, sampledPixel, flags; float u; };
+const int kLpValid = 1, kLpNeedsT = 2;
+
+// ComputeInitialSample with the shadow ray of the next-event estimate deferred to the network
+// and every resampling uniform drawn up front (the random stream does not depend on T)
+static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf, float preTr, Rng& sg, LpVertex* rec, f3* extra,
+                                    float* queries /* [maxBounces][8] */) {
+    const Scene& sc = *c.sc;
+    const SamplingOptions& options = c.initial;
+    const int maxBounces = c.maxBounces;
+    float pathPdf = 1.f, pathPHat = 1.f;
+    float primaryScatterDepth = 0;
+    const f3 sigma_s = sc.med.sigma_s, sigma_a = sc.med.sigma_a;
+    const float sigma_t = sc.med.sigma_t;
+    int bounce = 0;
+    for (; bounce < maxBounces; bounce++) {
+        Reservoir out = createNewReservoir();
+        out.M = 1;
+        float curHitDist, pdfDist = 0, Tr;
+        MediumInteraction mi;
+        if (bounce >= 1) {
+            int curMip = options.visibilityMipLevel;
+            if (c.o->mInitialUseCoarserGridForIndirectBounce)
+                curMip = std::min((options.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + sc.med.numMips - 1, curMip + 1);
+            float hd[4], pd[4], trs[4];
+            SampleMediumAnalyticGeneric(sc, ray, sg, options.visibilityUseLinearSampler, hd, curMip, pd, trs, 1);
+            curHitDist = hd[0]; pdfDist = pd[0]; Tr = trs[0];
+        } else {
+            curHitDist = preHit; pdfDist = prePdf; Tr = preTr;
+        }
+        mi.p = ray.at(curHitDist); mi.wo = -ray.dir; mi.g = sc.med.g; mi.isValid = curHitDist != kRayTMax;
+        pathPdf *= pdfDist;
+        bool hitEmpty = false;
+        float actualVolumeDensity = 0.f;
+        if (bounce == 0) {
+            if (maxBounces > 1) out.sampledPixel = encodeMaxIndirectBounces(out.sampledPixel, 0);
+            out.depth = mi.isValid ? curHitDist : kRayTMax;
+            primaryScatterDepth = out.depth;
+        } else if (maxBounces > 1) {
+            out.sampledPixel = encodeMaxIndirectBounces(out.sampledPixel, bounce);
+            extra[bounce - 1] = encodeWiDist(ray.dir, !mi.isValid ? kRayTMax : curHitDist);
+        }
+        out.p_y = pathPdf;
+        if (mi.isValid) actualVolumeDensity = DensityWorldSpace(sc, mi.p, 0);
+        if ((!mi.isValid && bounce > 0) || (mi.isValid && actualVolumeDensity == 0)) {
+            out.p_y = 0.f; out.runningSum = 0.f; hitEmpty = true;
+        }
+        int flags = kLpValid;
+        float pdfDir = 1.f;
+        queries[bounce * 8 + 6] = -1.f;
+        if (!hitEmpty) {
+            if (mi.isValid) {
+                f3 albedo = sigma_s / sigma_t;
+                out.lightID = -1; out.lightUV[0] = 0; out.lightUV[1] = 0;
+                float outLightPdf = 0.f;
+                f3 Ld = mk3(0.f), Le = mk3(0.f);
+                f3 one_minus_albedo = mk3(1.f) - albedo;
+                SceneLightSample ls;
+                bool lv = sampleSceneLights(sc, mi.p, options.useEnvironmentLights, options.useAnalyticLights, sg, ls, out.lightID, out.lightUV);
+                if (lv) {
+                    outLightPdf = ls.pdfArea;
+                    float p = phaseFunction(mi, mi.wo, ls.dir);
+                    Ld = mk3(0.f) + p * ls.Li / 1.f;
+                }
+                f3 wo = -ray.dir, wi = mk3(0.f);
+                if (maxBounces > 1) {
+                    float u0 = next1D(sg), u1 = next1D(sg);
+                    pdfDir = Sample_p(mi, wo, wi, u0, u1);
+                }
+                float p_src = out.p_y;
+                {
+                    float emissionRatio = luminance(one_minus_albedo * Le) / (luminance(one_minus_albedo * Le) + luminance(albedo * Ld));
+                    if (isnan_(emissionRatio)) emissionRatio = 0.f;
+                    if (next1D(sg) < emissionRatio) { p_src *= emissionRatio; out.lightID = kSelfEmissionLightID; }
+                    else p_src *= outLightPdf * (1 - emissionRatio);
+                }
+                out.runningSum = p_src == 0.f ? 0.f : 1.f;
+                out.p_y = p_src;
+                {
+                    float p_y;
+                    pathPHat *= Tr;
+                    pathPHat *= actualVolumeDensity;
+                    const bool emis = out.lightID == kSelfEmissionLightID;
+                    if (emis) p_y = pathPHat * luminance(sigma_a * Le);
+                    else p_y = pathPHat * luminance(sigma_s * Ld * outLightPdf);
+                    pathPHat *= luminance(sigma_s) * pdfDir;
+                    if (out.runningSum > 0.f) {
+                        if (!emis && lv && options.lightSamples != 0 && p_y != 0.f) {
+                            flags |= kLpNeedsT;
+                            out.runningSum = out.p_y;
+                            out.p_y = p_y;
+                            float* q = queries + bounce * 8;
+                            q[0] = mi.p.x; q[1] = mi.p.y; q[2] = mi.p.z; q[3] = ls.rayDir.x; q[4] = ls.rayDir.y; q[5] = ls.rayDir.z;
+                            q[6] = ls.rayDistance; q[7] = 0.f;
+                        } else {
+                            out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+                            if (emis && bounce > 0) {
+                                encodeEmissivePosition(mi.p, out.lightID, out.lightUV);
+                                p_y /= (curHitDist * curHitDist);
+                                out.sampledPixel = encodePathTag(out.sampledPixel, 1);
+                            }
+                            out.p_y = p_y;
+                        }
+                    }
+                }
+                pathPdf *= pdfDir;
+                if (maxBounces > 1 && bounce < maxBounces - 1) {
+                    ray = Ray{mi.p, wi, 0, kRayTMax};
+                    if (c.o->mInitialUseRussianRoulette && bounce >= 2) {
+                        if (next1D(sg) < albedo.x) pathPdf *= albedo.x;
+                        else hitEmpty = true;
+                    }
+                }
+            } else {
+                f3 Le = envEval(sc, ray.dir);
+                pathPHat *= Tr;
+                float p_y = pathPHat * luminance(Le);
+                out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+                out.p_y = p_y;
+                hitEmpty = true;
+            }
+        }
+        const float ub = maxBounces > 1 ? next1D(sg) : 0.f;
+        rec[bounce] = LpVertex{out.runningSum, out.p_y, out.lightUV[0], out.lightUV[1], out.lightID, out.sampledPixel, flags, ub};
+        if (hitEmpty) { bounce++; break; }
+    }
+    for (int b = bounce; b < maxBounces; ++b) { rec[b].flags = 0; queries[b * 8 + 6] = -1.f; }
+    return primaryScatterDepth;
+}
+
+// ---------------------------------------------------------------------------------------
 // evaluate_F_ family (ReSTIRHelper.slang:91-496)
 // ---------------------------------------------------------------------------------------
 struct ExtraProvider {        // StructuredBuffer/Array data providers (ArrayDataProvider.slang)
@@ -1378,6 +1670,13 @@ struct Oracle {
     std::vector<float> color;          // perPixelColor[0] (reference mode), rgba
     int lastMaxBounces = 0;
 
+    // learned target: network parameters and box, optional externally supplied T per vertex
+    // slot, and the frame's per-slot queries and training samples (exports for the tests)
+    std::vector<float> lpParams;
+    float lpBmin[3] = {0, 0, 0}, lpBinv[3] = {1, 1, 1};
+    std::vector<float> lpTIn;
+    std::vector<float> lpQueries, lpTrain, lpTUsed;
+
     int curPass = 0;     // 0 features, 1 initial, 2 temporal, 3 spatial, 4 final, 5 reference
     template <class F>
     void forRows(F f) {
@@ -1493,6 +1792,160 @@ struct Oracle {
             }
             if (cl.loopLimit) ll = true;
         });
+        if (ll) loopLimit = true;
+    }
+
+    // The initial pass with the learned target: candidates recorded with deferred shadow rays,
+    // T per query slot from lpTIn (when supplied) or the CPU network, then resampling of the
+    // records and the rest of TraceRays
+    void passTraceRaysLP(Ctx& c, const CamFrame& cam, int numTotalRounds) {
+        const int mb = c.maxBounces, M = opts.mInitialM;
+        const size_t N = (size_t)W * H;
+        lpQueries.assign((size_t)M * mb * N * 8, 0.f);
+        lpTUsed.assign((size_t)M * mb * N, 0.f);
+        const bool haveT = lpTIn.size() == (size_t)M * mb * N;
+        std::atomic<bool> ll(false);
+        forRows([&](int y) {
+            Ctx cl = c;
+            std::vector<LpVertex> rec((size_t)M * mb);
+            std::vector<f3> ex((size_t)M * std::max(mb - 1, 1));
+            std::vector<float> crec((size_t)M * 2), q((size_t)mb * 8);
+            for (int x = 0; x < W; ++x) {
+                Rng sg = rng_create((uint32_t)x, (uint32_t)y, (uint32_t)(numTotalRounds * frameCount));
+                const size_t pid = (size_t)y * W + x;
+                Ray ray{cam.posW, normalize(rayDirPinhole(cam, x, y, W, H)), 0.f, kRayTMax};
+                int rounds = (M + 3) / 4, cid = 0;
+                for (int roundId = 0; roundId < rounds; roundId++) {
+                    float hd[4] = {0, 0, 0, 0}, pd[4] = {0, 0, 0, 0}, trs[4] = {0, 0, 0, 0};
+                    int rs = roundId == rounds - 1 ? (M - 4 * (rounds - 1)) : 4;
+                    SampleMediumAnalyticGeneric(sc, ray, sg, c.initial.visibilityUseLinearSampler, hd, c.initial.visibilityMipLevel, pd, trs, rs);
+                    for (int sid = 0; sid < rs; sid++, cid++) {
+                        float depth = ComputeInitialSampleLP(cl, ray, hd[sid], pd[sid], trs[sid], sg, &rec[(size_t)cid * mb],
+                                                             &ex[(size_t)cid * std::max(mb - 1, 1)], q.data());
+                        crec[cid * 2] = depth;
+                        crec[cid * 2 + 1] = next1D(sg);
+                        for (int b = 0; b < mb; ++b) {
+                            const size_t slot = (size_t)(cid * mb + b) * N + pid;
+                            if (rec[(size_t)cid * mb + b].flags & kLpNeedsT) {
+                                memcpy(&lpQueries[slot * 8], &q[b * 8], 8 * sizeof(float));
+                                float t;
+                                if (haveT) t = lpTIn[slot];
+                                else {
+                                    float act[5][64];
+                                    float o = lpo::forward(lpParams.data(), &q[b * 8], &q[b * 8 + 3], lpBmin, lpBinv, act);
+                                    t = lpo::predict(o, opts.mLearnedTFloor);
+                                }
+                                lpTUsed[slot] = t;
+                            } else {
+                                lpQueries[slot * 8 + 6] = -1.f;
+                            }
+                        }
+                    }
+                }
+                // select
+                f3 finalExtra[3] = {mk3(0.f), mk3(0.f), mk3(0.f)};
+                Reservoir fin = createNewReservoir();
+                for (int ci = 0; ci < M; ++ci) {
+                    Reservoir comb = createNewReservoir();
+                    for (int b = 0; b < mb; ++b) {
+                        const LpVertex& v = rec[(size_t)ci * mb + b];
+                        if (!(v.flags & kLpValid)) break;
+                        Reservoir out = createNewReservoir();
+                        out.M = 1; out.depth = crec[ci * 2];
+                        out.runningSum = v.a; out.p_y = v.b; out.lightUV[0] = v.uv0; out.lightUV[1] = v.uv1;
+                        out.lightID = v.lightID; out.sampledPixel = v.sampledPixel;
+                        if (v.flags & kLpNeedsT) {
+                            float p_y = v.b * lpTUsed[(size_t)(ci * mb + b) * N + pid];
+                            out.runningSum = v.a == 0.f ? 0.f : p_y / v.a;
+                            out.p_y = p_y;
+                        }
+                        if (mb > 1) simpleResampleStepU(out, comb, v.u);
+                        else comb = out;
+                    }
+                    if (mb > 1) comb.M = 1;
+                    bool sel = simpleResampleStepU(comb, fin, crec[ci * 2 + 1]);
+                    if (sel && mb > 1) {
+                        int mib = decodeMaxIndirectBounces(fin.sampledPixel, mb);
+                        for (int b = 0; b < mib; b++) finalExtra[b] = ex[(size_t)ci * (mb - 1) + b];
+                    }
+                }
+                ExtraProvider prov{finalExtra};
+                float p_hat = evaluate_P_hat(cl, ray, sg, prov, c.spatial, fin);
+                if (fin.runningSum > 0.f) {
+                    fin.runningSum *= fin.p_y == 0.f ? 0.f : p_hat / fin.p_y;
+                    fin.p_y = p_hat;
+                }
+                fin.extraBounceStartId = mb > 1 ? (int)pid * (mb - 1) : 0;
+                perPixel[0][pid] = fin;
+                if (mb > 1) {
+                    int mib = decodeMaxIndirectBounces(fin.sampledPixel, mb);
+                    for (int b = 0; b < mib; b++) extraPP[0][(size_t)fin.extraBounceStartId + b] = finalExtra[b];
+                }
+            }
+            if (cl.loopLimit) ll = true;
+        });
+        if (ll) loopLimit = true;
+    }
+
+    // training samples of the network for this frame (stream seed as the product derives it)
+    void passTrainGenLP(Ctx& c, const CamFrame& cam) {
+        const int S = opts.mLearnedTrainSamples, mb = c.maxBounces;
+        lpTrain.assign((size_t)std::max(S, 0) * 8, 0.f);
+        const uint32_t seed = 0x80000000u | ((opts.mLearnedSeed * 0x9E3779B9u + (uint32_t)frameCount) & 0x7FFFFFFFu);
+        const int rows = (S + 255) / 256;
+        std::atomic<int> next(0);
+        std::atomic<bool> ll(false);
+        int nt = numThreads > 0 ? numThreads : (int)std::thread::hardware_concurrency();
+        auto work = [&]() {
+            Ctx cl = c;
+            for (int r; (r = next.fetch_add(1)) < rows;) {
+                for (int i = r * 256; i < std::min(S, r * 256 + 256); ++i) {
+                    Rng sg = rng_create((uint32_t)i & 0x3FFFu, (uint32_t)i >> 14, seed);
+                    MediumInteraction mi;
+                    mi.isValid = false;
+                    bool ok = false;
+                    for (int att = 0; att < 8 && !ok; att++) {
+                        int px = std::min(W - 1, (int)(next1D(sg) * (float)W));
+                        int py = std::min(H - 1, (int)(next1D(sg) * (float)H));
+                        int depth = std::min(mb - 1, (int)(next1D(sg) * (float)mb));
+                        Ray ray{cam.posW, normalize(rayDirPinhole(cam, px, py, W, H)), 0.f, kRayTMax};
+                        ok = true;
+                        for (int b = 0; b <= depth; b++) {
+                            mi.isValid = false;
+                            SampleMediumSuperVoxelGeneric(sc, ray, sg, mi, 0, cl.loopLimit);
+                            if (!mi.isValid) { ok = false; break; }
+                            if (b < depth) {
+                                f3 wi;
+                                float u0 = next1D(sg), u1 = next1D(sg);
+                                Sample_p(mi, -ray.dir, wi, u0, u1);
+                                ray = Ray{mi.p, wi, 0, kRayTMax};
+                            }
+                        }
+                    }
+                    SceneLightSample ls;
+                    if (ok) {
+                        int idx; float uv[2];
+                        ok = sampleSceneLights(sc, mi.p, c.initial.useEnvironmentLights, c.initial.useAnalyticLights, sg, ls, idx, uv);
+                    }
+                    float* o = &lpTrain[(size_t)i * 8];
+                    if (ok) {
+                        Ray sr{mi.p, ls.rayDir, 0, ls.rayDistance};
+                        float t = computeVisibility(sc, sr, sg, 1, 0, true, VR_TRACK_RESIDUAL_RATIO, 1.f);
+                        o[0] = mi.p.x; o[1] = mi.p.y; o[2] = mi.p.z; o[3] = ls.rayDir.x; o[4] = ls.rayDir.y; o[5] = ls.rayDir.z;
+                        o[6] = ls.rayDistance; o[7] = t;
+                    } else {
+                        o[6] = -1.f;
+                    }
+                }
+            }
+            if (cl.loopLimit) ll = true;
+        };
+        if (nt <= 1) work();
+        else {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nt; ++t) th.emplace_back(work);
+            for (auto& t : th) t.join();
+        }
         if (ll) loopLimit = true;
     }
 
@@ -1840,6 +2293,9 @@ struct Oracle {
                 }
                 if (cl.loopLimit) loopLimit = true;
             });
+        } else if (opts.mUseLearnedPHat && (opts.mEnableTemporalReuse || opts.mEnableSpatialReuse)) {
+            if (opts.mLearnedTrainSamples > 0) passTrainGenLP(c, cam);
+            passTraceRaysLP(c, cam, numTotalRounds);
         } else {
             passTraceRays(c, cam, numTotalRounds);
         }
@@ -2078,6 +2534,35 @@ void vro_xoshiro(const uint32_t seed[4], int draws, uint32_t* out) {
 void vro_splitmix(uint64_t seed, int draws, uint64_t* out) {
     uint64_t st = seed;
     for (int j = 0; j < draws; ++j) out[j] = splitmix64_next(st);
+}
+
+// learned target (test infrastructure)
+void vro_set_net(void* h, const float* params, const float bmin[3], const float binv[3]) {
+    Oracle* p = (Oracle*)h;
+    p->lpParams.assign(params, params + oracle::lpo::kParams);
+    for (int i = 0; i < 3; ++i) { p->lpBmin[i] = bmin[i]; p->lpBinv[i] = binv[i]; }
+}
+void vro_set_lp_T(void* h, const float* T, int64_t n) {
+    Oracle* p = (Oracle*)h;
+    if (!T || n <= 0) p->lpTIn.clear();
+    else p->lpTIn.assign(T, T + n);
+}
+// which 0: per-slot queries (8 floats, tmax = -1 where none), 1: T used per slot, 2: training samples
+int64_t vro_export_lp(void* h, int which, float* out, int64_t cap) {
+    Oracle* p = (Oracle*)h;
+    const std::vector<float>& v = which == 0 ? p->lpQueries : which == 1 ? p->lpTUsed : p->lpTrain;
+    if (out && cap >= (int64_t)v.size()) memcpy(out, v.data(), v.size() * sizeof(float));
+    return (int64_t)v.size();
+}
+void vro_net_forward(const float* params, const float bmin[3], const float binv[3], float floor_, const float* q, int n, float* out) {
+    for (int i = 0; i < n; ++i) {
+        float act[5][64];
+        float o = oracle::lpo::forward(params, q + (size_t)i * 8, q + (size_t)i * 8 + 3, bmin, binv, act);
+        out[i] = oracle::lpo::predict(o, floor_);
+    }
+}
+void vro_net_gradients(const float* params, const float bmin[3], const float binv[3], const float* samples, int n, float* grads, float* loss) {
+    oracle::lpo::gradients(params, samples, n, bmin, binv, grads, loss);
 }
 
 }  // extern "C"

@@ -21,7 +21,7 @@ LIB = PKG / "_lib" / "libvrestir.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-v"]
-HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h", "vr_noalloc.h"]
+HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h", "vr_noalloc.h", "vr_lp.h", "vr_lp_kernels.cuh", "lp_net.h"]
 
 
 def _nvcc():

@@ -41,6 +41,8 @@ class Options(C.Structure):
         ("mSpatialSampleCount", _i32), ("mSpatialMISMethod", _u32), ("mFinalLightSamples", _i32),
         ("mFinalVisibilitySamples", _i32), ("mFinalVisibilityTrackingMethod", _u32),
         ("mFinalLightTrackingMethod", _u32), ("mFinalTStepScale", _f32),
+        ("mUseLearnedPHat", _i32), ("mLearnedTrainSamples", _i32), ("mLearnedBatch", _i32),
+        ("mLearnedLearningRate", _f32), ("mLearnedTFloor", _f32), ("mLearnedSeed", _u32),
     ]
 
     def as_dict(self):
@@ -125,7 +127,15 @@ SIGNATURES = {
     "vr_selftest_math": (_i32, [_i32, C.POINTER(_f32), C.POINTER(_f32), C.POINTER(_f32), _i32]),
     "vr_selftest_rng": (_i32, [C.POINTER(_u32), _i32, _i32, C.POINTER(_f32)]),
     "vr_selftest_umma": (_i32, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(_f32), _i32]),
+    "vr_net_get_params": (_i32, [_P, C.POINTER(_f32)]),
+    "vr_net_set_params": (_i32, [_P, C.POINTER(_f32)]),
+    "vr_net_infer": (_i32, [_P, _P, _i32, _P, _P]),
+    "vr_net_gradients": (_i32, [_P, _P, _i32, C.POINTER(_f32), C.POINTER(_f32)]),
+    "vr_net_train_step": (_i32, [_P, _P, _i32, C.POINTER(_f32)]),
+    "vr_export_learned": (_i32, [_P, _i32, _P, C.c_size_t, C.POINTER(C.c_int64)]),
 }
+
+NET_PARAMS = 16705
 
 _LIB = None
 

@@ -18,7 +18,9 @@
 #include <vector>
 
 #include "../../include/vrestir.h"
+#include "lp_net.h"
 #include "vr_kernels.cuh"
+#include "vr_lp.h"
 #include "vr_volume.h"
 
 // per-path-length kernel objects (frame_kernels.cu compiled with VR_MB = 1..4)
@@ -28,9 +30,19 @@ namespace vrk {
     void launch_initial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, dim3, dim3, cudaStream_t);     \
     void launch_spatial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::SpatialParams&, dim3, dim3, cudaStream_t); \
     void launch_final_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, int, dim3, dim3, cudaStream_t);  \
-    void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);
+    void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);        \
+    void launch_lp_generate_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
+    void launch_lp_select_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
+    void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);
 VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 #undef VR_DECL
+// the network kernels (lp.cu)
+cudaError_t net_setup();
+void launch_net_infer(const vrd::NetView&, const float4*, int, const int*, float*, int, int*, int, cudaStream_t);
+void launch_net_train(const vrd::NetView&, const float4*, int, float*, float*, cudaStream_t);
+void launch_net_reduce_adam(const float*, int, const float*, float*, float*, float*, float*, float*, uint16_t*, float*, float, float, float, int,
+                            cudaStream_t);
+void launch_net_pack(const float*, uint16_t*, float*, cudaStream_t);
 }
 
 using vr::f3;
@@ -228,6 +240,22 @@ struct vr_context {
     int launches = 0;
     int64_t h2d = 0, d2h = 0;
     int* status = nullptr;    // device status word
+    // learned target: network (FP32 master weights, Adam moments, BF16 copy) and the buffers
+    // of the split initial pass
+    float *netW = nullptr, *netM = nullptr, *netV = nullptr, *netG = nullptr, *netBias = nullptr;
+    uint16_t* netWbf = nullptr;
+    float *netPart = nullptr, *netLossPart = nullptr, *netScalar = nullptr;
+    int netPartRows = 0;
+    bool netReady = false;
+    int64_t adamStep = 0;
+    float netBmin[3] = {0, 0, 0}, netBinv[3] = {1, 1, 1};
+    int numSMs = 0;
+    vrd::LpBuffers lp{};
+    size_t lpSlots = 0;            // allocated vertex slots (M * MB * N)
+    int lpM = 0, lpMB = 0;
+    float* stepLoss = nullptr;     // loss of each Adam step of the last frame
+    int stepLossCap = 0, lastSteps = 0;
+    bool lpFrameDone = false;
 };
 
 static void free_buffers(vr_context* c) {
@@ -267,6 +295,139 @@ static int alloc_buffers(vr_context* c) {
     return VR_OK;
 }
 
+// ---- learned target: network state and the buffers of the split initial pass ----
+static void free_lp(vr_context* c) {
+    cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.ex); cudaFree(c->lp.T);
+    cudaFree(c->lp.query); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
+    c->lp = vrd::LpBuffers{};
+    c->lpSlots = 0; c->lpM = 0; c->lpMB = 0;
+}
+static void free_net(vr_context* c) {
+    float* fs[] = {c->netW, c->netM, c->netV, c->netG, c->netBias, c->netPart, c->netLossPart, c->netScalar, c->stepLoss};
+    for (float* f : fs) cudaFree(f);
+    cudaFree(c->netWbf);
+    c->netW = c->netM = c->netV = c->netG = c->netBias = c->netPart = c->netLossPart = c->netScalar = c->stepLoss = nullptr;
+    c->netWbf = nullptr;
+    c->netPartRows = 0; c->stepLossCap = 0; c->netReady = false;
+}
+
+// He-uniform hidden weights from a SplitMix64 stream, small output weights (T starts near 1),
+// zero biases; layer 0's four pad columns stay zero
+static void net_init_params(uint32_t seed, std::vector<float>& w) {
+    w.assign(lpn::kParams, 0.f);
+    uint64_t st = 0x6C7E3A91D2B54F08ull ^ ((uint64_t)seed << 17);
+    auto uni = [&]() { return (float)((vr::splitmix64_next(st) >> 40) * (1.0 / 16777216.0)) * 2.f - 1.f; };
+    for (int l = 0; l < lpn::kLayers; ++l) {
+        const int fanIn = l == 0 ? lpn::kIn : lpn::kHid;
+        const float bound = std::sqrt(6.f / (float)fanIn);
+        for (int r = 0; r < lpn::kHid; ++r)
+            for (int k = 0; k < lpn::kInPad; ++k) {
+                float u = uni();
+                w[lpn::w_off(l) + r * lpn::kInPad + k] = (l == 0 && k >= lpn::kIn) ? 0.f : u * bound;
+            }
+    }
+    const float ob = 0.1f * std::sqrt(6.f / (float)lpn::kHid);
+    for (int k = 0; k < lpn::kHid; ++k) w[lpn::kOutW + k] = uni() * ob;
+}
+
+static int net_alloc(vr_context* c, int partRows) {
+    if (!c->netW) {
+        c->netW = dalloc<float>(lpn::kParamsPad); c->netM = dalloc<float>(lpn::kParamsPad); c->netV = dalloc<float>(lpn::kParamsPad);
+        c->netG = dalloc<float>(lpn::kParamsPad); c->netBias = dalloc<float>(320); c->netWbf = dalloc<uint16_t>(5 * 4096);
+        c->netScalar = dalloc<float>(4);
+        if (!c->netW || !c->netM || !c->netV || !c->netG || !c->netBias || !c->netWbf || !c->netScalar) {
+            c->err = "out of device memory (network)"; return VR_ERR_OOM;
+        }
+        if (vrk::net_setup() != cudaSuccess) { c->err = "network kernel setup failed"; return VR_ERR_CUDA; }
+        cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, 0);
+        if (c->numSMs <= 0) c->numSMs = 1;
+    }
+    if (partRows > c->netPartRows) {
+        cudaFree(c->netPart); cudaFree(c->netLossPart);
+        c->netPart = dalloc<float>((size_t)partRows * lpn::kParamsPad);
+        c->netLossPart = dalloc<float>(partRows);
+        if (!c->netPart || !c->netLossPart) { c->netPartRows = 0; c->err = "out of device memory (network gradients)"; return VR_ERR_OOM; }
+        c->netPartRows = partRows;
+    }
+    return VR_OK;
+}
+
+static int net_upload(vr_context* c, const float* host) {
+    cudaMemcpy(c->netW, host, lpn::kParams * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemset(c->netM, 0, lpn::kParamsPad * sizeof(float));
+    cudaMemset(c->netV, 0, lpn::kParamsPad * sizeof(float));
+    vrk::launch_net_pack(c->netW, c->netWbf, c->netBias, 0);
+    if (cudaDeviceSynchronize() != cudaSuccess) { c->err = "network upload failed"; return VR_ERR_CUDA; }
+    c->adamStep = 0;
+    c->netReady = true;
+    return VR_OK;
+}
+
+static int net_ensure(vr_context* c, int partRows) {
+    int r = net_alloc(c, std::max(partRows, 1));
+    if (r) return r;
+    if (!c->netReady) {
+        std::vector<float> w;
+        net_init_params(c->opts.mLearnedSeed, w);
+        return net_upload(c, w.data());
+    }
+    return VR_OK;
+}
+
+static vrd::NetView net_view(const vr_context* c) {
+    vrd::NetView v;
+    v.wbf = c->netWbf; v.bias = c->netBias;
+    for (int i = 0; i < 3; ++i) { v.bmin[i] = c->netBmin[i]; v.binv[i] = c->netBinv[i]; }
+    v.floor_ = c->opts.mLearnedTFloor;
+    return v;
+}
+
+static bool lp_active(const vr_context* c) {
+    const vr_options& o = c->opts;
+    return o.mUseLearnedPHat && !o.mUseReference && (o.mEnableTemporalReuse || o.mEnableSpatialReuse);
+}
+
+static int lp_alloc(vr_context* c) {
+    const vr_options& o = c->opts;
+    const size_t N = (size_t)c->W * c->H;
+    const int M = o.mInitialM, MB = o.mMaxBounces;
+    const size_t slots = (size_t)M * MB * N;
+    if (slots >= (size_t)INT32_MAX) { c->err = "mInitialM * mMaxBounces * pixels must stay below 2^31 with the learned target"; return VR_ERR_INVALID_ARG; }
+    const int S = std::max(0, o.mLearnedTrainSamples);
+    int r = net_ensure(c, (std::min(std::max(o.mLearnedBatch, 1), std::max(S, 1)) + 127) / 128);
+    if (r) return r;
+    if (c->lpSlots != slots || c->lpM != M || c->lpMB != MB || c->lp.trainCount != S) {
+        free_lp(c);
+        c->lp.vrecA = dalloc<float4>(slots);
+        c->lp.vrecB = dalloc<int4>(slots);
+        c->lp.crec = dalloc<float2>((size_t)M * N);
+        c->lp.ex = dalloc<float4>((size_t)M * std::max(MB - 1, 1) * N);
+        c->lp.T = dalloc<float>(slots);
+        c->lp.query = dalloc<float4>(2 * slots);
+        c->lp.qcount = dalloc<int>(1);
+        c->lp.rng = dalloc<uint4>(N);
+        c->lp.train = dalloc<float4>(2 * (size_t)std::max(S, 1));
+        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qcount || !c->lp.rng || !c->lp.train) {
+            free_lp(c);
+            c->err = "out of device memory (learned-target buffers)";
+            return VR_ERR_OOM;
+        }
+        cudaMemset(c->lp.T, 0, slots * sizeof(float));
+        cudaMemset(c->lp.qcount, 0, sizeof(int));
+        c->lp.qcapacity = (int)slots;
+        c->lp.trainCount = S;
+        c->lpSlots = slots; c->lpM = M; c->lpMB = MB;
+    }
+    const int steps = S > 0 ? std::max(1, S / std::max(1, std::min(o.mLearnedBatch, S))) : 0;
+    if (steps > c->stepLossCap) {
+        cudaFree(c->stepLoss);
+        c->stepLoss = dalloc<float>(steps);
+        if (!c->stepLoss) { c->stepLossCap = 0; c->err = "out of device memory (loss log)"; return VR_ERR_OOM; }
+        c->stepLossCap = steps;
+    }
+    return VR_OK;
+}
+
 static bool options_valid(const vr_options* o, std::string& why) {
     if (o->mMaxBounces < 1 || o->mMaxBounces > VR_MAX_BOUNCES) { why = "mMaxBounces must be in [1, 4]"; return false; }
     if (o->mInitialM < 1 || o->mInitialM > 4096) { why = "mInitialM must be in [1, 4096]"; return false; }
@@ -282,6 +443,13 @@ static bool options_valid(const vr_options* o, std::string& why) {
                           o->mFinalVisibilityTrackingMethod, o->mFinalLightTrackingMethod};
     for (uint32_t m : methods) if (m > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown tracking method"; return false; }
     if (o->mTemporalReprojectionMode > VR_REPROJ_NO_BACKGROUND) { why = "unknown reprojection mode"; return false; }
+    if (o->mUseLearnedPHat) {
+        if (!o->mEnableTemporalReuse && !o->mEnableSpatialReuse) { why = "mUseLearnedPHat needs temporal or spatial reuse"; return false; }
+        if (o->mLearnedTrainSamples < 0 || o->mLearnedTrainSamples > (1 << 26)) { why = "mLearnedTrainSamples must be in [0, 2^26]"; return false; }
+        if (o->mLearnedBatch < 1 || o->mLearnedBatch > (1 << 20)) { why = "mLearnedBatch must be in [1, 2^20]"; return false; }
+        if (!(o->mLearnedLearningRate >= 0.f) || !(o->mLearnedLearningRate < 1.f)) { why = "mLearnedLearningRate must be in [0, 1)"; return false; }
+        if (!(o->mLearnedTFloor > 0.f) || !(o->mLearnedTFloor <= 1.f)) { why = "mLearnedTFloor must be in (0, 1]"; return false; }
+    }
     return true;
 }
 
@@ -308,6 +476,7 @@ static bool slots_present(const vr_context* c, std::string& why) {
 
 template <int MB>
 static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st);
+static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st);
 
 extern "C" {
 
@@ -354,6 +523,12 @@ void vr_options_default(vr_options* o) {
     o->mFinalVisibilityTrackingMethod = VR_TRACK_ANALYTIC;
     o->mFinalLightTrackingMethod = VR_TRACK_ANALYTIC;
     o->mFinalTStepScale = 0.2f;
+    o->mUseLearnedPHat = 0;
+    o->mLearnedTrainSamples = 1 << 20;
+    o->mLearnedBatch = 16384;
+    o->mLearnedLearningRate = 1e-3f;
+    o->mLearnedTFloor = 0.02f;
+    o->mLearnedSeed = 1;
 }
 
 // ---- volumes ----
@@ -438,6 +613,8 @@ vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int
 void vr_destroy(vr_context* c) {
     if (!c) return;
     free_buffers(c);
+    free_lp(c);
+    free_net(c);
     for (void* p : c->sceneAllocs) cudaFree(p);
     for (void* p : c->envAllocs) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
@@ -514,6 +691,10 @@ int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
     c->scene.superDiag = v.supervoxel_diag;
     c->scene.numMips = v.num_mips;
     c->numMips = v.num_mips;
+    for (int i = 0; i < 3; ++i) {
+        c->netBmin[i] = v.world_min[i];
+        c->netBinv[i] = 1.f / ((float)v.res * v.voxel_size);
+    }
     c->hasVolume = true;
     c->optionsChanged = true;
     return VR_OK;
@@ -617,6 +798,7 @@ static int prepare_frame(vr_context* c, const vr_camera* cam) {
     if (c->opts.mUseEnvironmentLights && !c->scene.hasEnv) { c->err = "mUseEnvironmentLights needs an environment map"; return VR_ERR_INVALID_ARG; }
     int r = alloc_buffers(c);
     if (r) return r;
+    if (lp_active(c) && (r = lp_alloc(c))) return r;
     if (c->optionsChanged) { c->frameCount = 0; c->temporalSampleAccumulated = 0; c->optionsChanged = false; }
     return VR_OK;
 }
@@ -805,13 +987,18 @@ int vr_last_timings(const vr_context* c, float* ms, int32_t max_entries, int32_t
 }
 int32_t vr_last_launch_count(const vr_context* c) { return c ? c->launches : 0; }
 
+// frame events: start, after training, after the initial stage, after the last kernel;
+// totals: 0 initial stage, 1 spatial/final stage, 2 network training
 static void drain_events(vr_context* c) {
     for (auto& v : c->pendingEv) {
         cudaEventSynchronize(v.back());
-        for (size_t i = 0; i + 1 < v.size() && i < 4; ++i) {
-            float t = 0.f;
-            cudaEventElapsedTime(&t, v[i], v[i + 1]);
-            c->totalMs[i] += t;
+        if (v.size() == 4) {
+            const int map[3][3] = {{1, 2, 0}, {2, 3, 1}, {0, 1, 2}};
+            for (auto& m : map) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, v[m[0]], v[m[1]]);
+                c->totalMs[m[2]] += t;
+            }
         }
         c->totalFrames++;
         for (auto e : v) c->freeEv.push_back(e);
@@ -826,6 +1013,90 @@ int vr_kernel_time_totals(vr_context* c, float* ms, int32_t max_entries, int32_t
     if (reset) { for (double& t : c->totalMs) t = 0; c->totalFrames = 0; }
     return VR_OK;
 }
+// ---- learned target: network ----
+int vr_net_get_params(vr_context* c, float* host) {
+    if (!c || !host) return VR_ERR_INVALID_ARG;
+    int r = net_ensure(c, 1);
+    if (r) return r;
+    if (cudaMemcpy(host, c->netW, lpn::kParams * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) return check_cuda(c, "network export");
+    return VR_OK;
+}
+int vr_net_set_params(vr_context* c, const float* host) {
+    if (!c || !host) return VR_ERR_INVALID_ARG;
+    for (int i = 0; i < lpn::kParams; ++i)
+        if (!(host[i] == host[i]) || vr::isinf_(host[i])) { c->err = "network parameters must be finite"; return VR_ERR_INVALID_ARG; }
+    int r = net_alloc(c, 1);
+    if (r) return r;
+    return net_upload(c, host);
+}
+int vr_net_infer(vr_context* c, const float* q, int32_t n, float* out, void* stream) {
+    if (!c || n < 0 || (n > 0 && (!q || !out))) return VR_ERR_INVALID_ARG;
+    int r = net_ensure(c, 1);
+    if (r) return r;
+    if (n == 0) return VR_OK;
+    vrk::launch_net_infer(net_view(c), (const float4*)q, n, nullptr, out, 0, c->status, c->numSMs, (cudaStream_t)stream);
+    return check_cuda(c, "network inference");
+}
+static int net_grad_common(vr_context* c, const float* samples, int32_t n, float* loss, bool update, float* grads) {
+    if (!c || !samples || n <= 0 || n > (1 << 22)) return VR_ERR_INVALID_ARG;
+    int r = net_ensure(c, (n + 127) / 128);
+    if (r) return r;
+    if (update) {
+        lp_train_steps(c, (const float4*)samples, n, 0);
+        c->launches -= 2;
+    } else {
+        vrk::launch_net_train(net_view(c), (const float4*)samples, n, c->netPart, c->netLossPart, 0);
+        vrk::launch_net_reduce_adam(c->netPart, (n + 127) / 128, c->netLossPart, c->netW, c->netM, c->netV, c->netG, c->netScalar, c->netWbf,
+                                    c->netBias, 0.f, 1.f, 1.f, 0, 0);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return check_cuda(c, "network training");
+    if (loss) cudaMemcpy(loss, update ? c->stepLoss : c->netScalar, sizeof(float), cudaMemcpyDeviceToHost);
+    if (grads) cudaMemcpy(grads, c->netG, lpn::kParams * sizeof(float), cudaMemcpyDeviceToHost);
+    return check_cuda(c, "network training");
+}
+int vr_net_gradients(vr_context* c, const float* samples, int32_t n, float* grads, float* loss) {
+    if (!grads) return VR_ERR_INVALID_ARG;
+    return net_grad_common(c, samples, n, loss, false, grads);
+}
+int vr_net_train_step(vr_context* c, const float* samples, int32_t n, float* loss) {
+    if (c && c->opts.mLearnedBatch < n) { c->err = "n exceeds mLearnedBatch"; return VR_ERR_INVALID_ARG; }
+    if (c && c->stepLossCap < 1) {
+        int r = net_alloc(c, (n + 127) / 128);
+        if (r) return r;
+        c->stepLoss = dalloc<float>(1);
+        if (!c->stepLoss) return VR_ERR_OOM;
+        c->stepLossCap = 1;
+    }
+    return net_grad_common(c, samples, n, loss, true, nullptr);
+}
+int vr_export_learned(vr_context* c, int32_t which, void* host, size_t bytes, int64_t* count) {
+    if (!c || !count) return VR_ERR_INVALID_ARG;
+    if (which == 4) {
+        *count = 6;
+        if (!host || bytes < 24) return VR_ERR_INVALID_ARG;
+        float* f = (float*)host;
+        for (int i = 0; i < 3; ++i) { f[i] = c->netBmin[i]; f[3 + i] = c->netBinv[i]; }
+        return VR_OK;
+    }
+    if (!c->lpFrameDone) { c->err = "no learned-target frame rendered yet"; return VR_ERR_STATE; }
+    if (cudaDeviceSynchronize() != cudaSuccess) return check_cuda(c, "export");
+    const void* src = nullptr;
+    size_t need = 0;
+    if (which == 0) { *count = (int64_t)c->lpSlots; src = c->lp.T; need = c->lpSlots * sizeof(float); }
+    else if (which == 1) {
+        int qc = 0;
+        cudaMemcpy(&qc, c->lp.qcount, sizeof(int), cudaMemcpyDeviceToHost);
+        *count = std::min(qc, c->lp.qcapacity);
+        src = c->lp.query; need = (size_t)*count * 32;
+    } else if (which == 2) { *count = c->lp.trainCount; src = c->lp.train; need = (size_t)c->lp.trainCount * 32; }
+    else if (which == 3) { *count = c->lastSteps; src = c->stepLoss; need = (size_t)c->lastSteps * sizeof(float); }
+    else return VR_ERR_INVALID_ARG;
+    if (!host) return VR_OK;
+    if (bytes < need) { c->err = "export buffer too small"; return VR_ERR_INVALID_ARG; }
+    if (need && cudaMemcpy(host, src, need, cudaMemcpyDeviceToHost) != cudaSuccess) return check_cuda(c, "export");
+    return VR_OK;
+}
+
 int vr_last_transfer_bytes(const vr_context* c, int64_t* h2d, int64_t* d2h) {
     if (!c || !h2d || !d2h) return VR_ERR_INVALID_ARG;
     *h2d = c->h2d;
@@ -861,6 +1132,49 @@ static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, 
 }
 
 template <int MB>
+static void launch_lp_generate(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
+    if (MB == 1) vrk::launch_lp_generate_1(P, B, L, g, b, st);
+    else if (MB == 2) vrk::launch_lp_generate_2(P, B, L, g, b, st);
+    else if (MB == 3) vrk::launch_lp_generate_3(P, B, L, g, b, st);
+    else vrk::launch_lp_generate_4(P, B, L, g, b, st);
+}
+template <int MB>
+static void launch_lp_select(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
+    if (MB == 1) vrk::launch_lp_select_1(P, B, L, g, b, st);
+    else if (MB == 2) vrk::launch_lp_select_2(P, B, L, g, b, st);
+    else if (MB == 3) vrk::launch_lp_select_3(P, B, L, g, b, st);
+    else vrk::launch_lp_select_4(P, B, L, g, b, st);
+}
+template <int MB>
+static void launch_lp_train_gen(const vrd::FrameParams& P, const vrd::LpBuffers& L, uint32_t seed, cudaStream_t st) {
+    if (MB == 1) vrk::launch_lp_train_gen_1(P, L, seed, st);
+    else if (MB == 2) vrk::launch_lp_train_gen_2(P, L, seed, st);
+    else if (MB == 3) vrk::launch_lp_train_gen_3(P, L, seed, st);
+    else vrk::launch_lp_train_gen_4(P, L, seed, st);
+}
+
+// seed of the training-sample streams of a frame
+static uint32_t lp_train_seed(uint32_t learnedSeed, int frameCount) { return 0x80000000u | ((learnedSeed * 0x9E3779B9u + (uint32_t)frameCount) & 0x7FFFFFFFu); }
+
+// one Adam step per batch over the frame's fresh training samples
+static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st) {
+    const vr_options& o = c->opts;
+    const int Bt = std::max(1, std::min(o.mLearnedBatch, S));
+    const int steps = std::max(1, S / Bt);
+    const vrd::NetView nv = net_view(c);
+    for (int k = 0; k < steps; ++k) {
+        vrk::launch_net_train(nv, samples + 2 * (size_t)k * Bt, Bt, c->netPart, c->netLossPart, st);
+        c->adamStep++;
+        const float c1 = (float)(1.0 - std::pow(0.9, (double)c->adamStep));
+        const float c2 = (float)(1.0 - std::pow(0.999, (double)c->adamStep));
+        vrk::launch_net_reduce_adam(c->netPart, (Bt + 127) / 128, c->netLossPart, c->netW, c->netM, c->netV, c->netG, c->stepLoss + k,
+                                    c->netWbf, c->netBias, o.mLearnedLearningRate, c1, c2, 1, st);
+        c->launches += 2;
+    }
+    c->lastSteps = steps;
+}
+
+template <int MB>
 static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st) {
     const vr_options& o = c->opts;
     dim3 grid((c->W + 7) / 8, (c->H + 15) / 16), block(128);
@@ -874,8 +1188,34 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         frameEv.push_back(e);
     };
     mark();
-    launch_initial<MB>(P, B, grid, block, st);
-    c->launches++;
+    cudaEvent_t afterTrain = nullptr;
+    const bool lpOn = lp_active(c);
+    if (lpOn) {
+        if (c->opts.mLearnedTrainSamples > 0) {
+            launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(c->opts.mLearnedSeed, c->frameCount), st);
+            c->launches++;
+            lp_train_steps(c, c->lp.train, c->opts.mLearnedTrainSamples, st);
+        } else {
+            c->lastSteps = 0;
+        }
+        if (c->nev < 10) cudaEventRecord(c->ev[c->nev++], st);
+    }
+    {
+        if (!c->freeEv.empty()) { afterTrain = c->freeEv.back(); c->freeEv.pop_back(); }
+        else cudaEventCreate(&afterTrain);
+        cudaEventRecord(afterTrain, st);
+    }
+    if (lpOn) {
+        cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+        launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
+        vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, 1, c->status, c->numSMs, st);
+        launch_lp_select<MB>(P, B, c->lp, grid, block, st);
+        c->launches += 3;
+        c->lpFrameDone = true;
+    } else {
+        launch_initial<MB>(P, B, grid, block, st);
+        c->launches++;
+    }
     mark();
     int totalRoundId = 0;
     bool temporal = !o.mUseReference && o.mEnableTemporalReuse;
@@ -913,6 +1253,7 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         mark();
     }
     c->finalBuf = totalRoundId % 2;
+    frameEv.insert(frameEv.begin() + 1, afterTrain);
     c->pendingEv.push_back(frameEv);
     if (c->pendingEv.size() > 512) drain_events(c);
 }

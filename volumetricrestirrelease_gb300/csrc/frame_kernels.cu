@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "vr_kernels.cuh"
+#include "vr_lp_kernels.cuh"
 
 #ifndef VR_MB
 #error "VR_MB must be defined (1..4)"
@@ -27,6 +28,18 @@ void VR_CAT(launch_final_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuf
 }
 void VR_CAT(launch_reference_, VR_MB)(const vrd::FrameParams& P, int first, int count, double* accum, dim3 g, dim3 b, cudaStream_t st) {
     vrd::k_reference<VR_MB><<<g, b, 0, st>>>(P, first, count, accum);
+}
+
+void VR_CAT(launch_lp_generate_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b,
+                                        cudaStream_t st) {
+    vrd::k_lp_generate<VR_MB><<<g, b, 0, st>>>(P, B, L);
+}
+void VR_CAT(launch_lp_select_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b,
+                                      cudaStream_t st) {
+    vrd::k_lp_select<VR_MB><<<g, b, 0, st>>>(P, B, L);
+}
+void VR_CAT(launch_lp_train_gen_, VR_MB)(const vrd::FrameParams& P, const vrd::LpBuffers& L, uint32_t seed, cudaStream_t st) {
+    vrd::k_lp_train_gen<VR_MB><<<(L.trainCount + 127) / 128, 128, 0, st>>>(P, L, seed);
 }
 
 }  // namespace vrk

@@ -1,0 +1,312 @@
+// vr_lp_kernels.cuh -- the initial pass with the learned target, split into generate and select
+// around the batched network evaluation, and the generation of the network's training samples.
+//
+// generate follows ComputeInitialSample (ComputeInitialSample.slang:4-395) and TraceRays
+// (TraceRays.cs.slang:104-198) step for step with two changes: the next-event estimate does not
+// march its shadow ray (SampleDirectLighting's visibility, VolumeUtils.slang:485-521), and every
+// resampling uniform is drawn at generation time whether or not the weight is positive, so the
+// random stream is independent of the predicted transmittance.
+#pragma once
+
+#include "vr_kernels.cuh"
+#include "vr_lp.h"
+
+namespace vrd {
+
+__device__ __forceinline__ bool resampleStepU(const Reservoir& r, Reservoir& s, float u) {
+    float w = r.runningSum;
+    s.M += r.M;
+    if (w <= 0.0f) return false;
+    s.runningSum += w;
+    bool sel = u * s.runningSum < w;
+    if (sel) copySample(r, s);
+    return sel;
+}
+
+// appends one transmittance query; the threads that reach this point together share one atomic
+__device__ __forceinline__ void lpAppendQuery(const LpBuffers& L, f3 x, f3 w, float tmax, int slot) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(L.qcount, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    const int idx = base + rank;
+    if (idx < L.qcapacity) {
+        L.query[2 * (size_t)idx] = make_float4(x.x, x.y, x.z, w.x);
+        L.query[2 * (size_t)idx + 1] = make_float4(w.y, w.z, tmax, __int_as_float(slot));
+    } else if (c_scene.status) {
+        atomicOr(c_scene.status, 2);
+    }
+}
+
+// one candidate path; writes the vertex records of candidate c of pixel pid and returns the
+// primary scattering depth
+template <int MB>
+static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray ray, float preHit, float prePdf, float preTr, vr::Rng& sg,
+                                                      const LpBuffers& L, int c, int pid) {
+    const SamplingOptions& o = P.initial;
+    const int N = P.N;
+    float pathPdf = 1.f, pathPHat = 1.f;
+    float primaryDepth = 0;
+    const f3 sigma_s = c_scene.sigma_s, sigma_a = c_scene.sigma_a;
+    const float sigma_t = c_scene.sigma_t;
+    int bounce = 0;
+    for (; bounce < MB; bounce++) {
+        Reservoir out = newReservoir();
+        out.M = 1;
+        float hitD, pdfDist = 0, Tr;
+        MediumInteraction mi;
+        if (bounce >= 1) {
+            int curMip = o.visibilityMipLevel;
+            if (P.useCoarser) curMip = min((o.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + c_scene.numMips - 1, curMip + 1);
+            float hd[4], pd[4], trs[4];
+            sampleDistances(ray, sg, o.visibilityUseLinearSampler != 0, curMip, 1, hd, pd, trs);
+            hitD = hd[0]; pdfDist = pd[0]; Tr = trs[0];
+        } else {
+            hitD = preHit; pdfDist = prePdf; Tr = preTr;
+        }
+        mi.p = at(ray, hitD); mi.wo = -ray.d; mi.g = c_scene.g; mi.valid = hitD != kRayTMax;
+        pathPdf *= pdfDist;
+        bool hitEmpty = false;
+        float density = 0.f;
+        if (bounce == 0) {
+            if (MB > 1) out.sampledPixel = encodeBounces(out.sampledPixel, 0);
+            out.depth = mi.valid ? hitD : kRayTMax;
+            primaryDepth = out.depth;
+        } else {
+            if (MB > 1) {
+                out.sampledPixel = encodeBounces(out.sampledPixel, bounce);
+                f3 w = mk3(ray.d.x, ray.d.y, !mi.valid ? kRayTMax : hitD);
+                if (ray.d.z < 0) w.z = -w.z;
+                L.ex[(size_t)(c * (MB - 1) + bounce - 1) * N + pid] = make_float4(w.x, w.y, w.z, 0.f);
+            }
+        }
+        out.p_y = pathPdf;
+        if (mi.valid) density = densityWorld(mi.p, 0);
+        if ((!mi.valid && bounce > 0) || (mi.valid && density == 0)) {
+            out.p_y = 0.f; out.runningSum = 0.f; hitEmpty = true;
+        }
+        int flags = kLpValid;
+        float pdfDir = 1.f;
+        if (!hitEmpty) {
+            if (mi.valid) {
+                f3 albedo = sigma_s / sigma_t;
+                out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
+                float lightPdf = 0.f;
+                f3 Le = mk3(0.f);
+                f3 oma = mk3(1.f) - albedo;
+                LightSample ls;
+                const bool lv = sampleLights(mi.p, o.useEnvironmentLights != 0, o.useAnalyticLights != 0, sg, ls, out.lightID, out.uv0, out.uv1);
+                f3 Ld = mk3(0.f);
+                if (lv) {
+                    lightPdf = ls.pdfArea;
+                    float ph = phaseF(mi, mi.wo, ls.dir);
+                    Ld = mk3(0.f) + ph * ls.Li / 1.f;
+                }
+                f3 wo = -ray.d, wi = mk3(0.f);
+                if (MB > 1) {
+                    float u0 = vr::next1D(sg), u1 = vr::next1D(sg);
+                    pdfDir = samplePhase(mi, wo, wi, u0, u1);
+                }
+                float p_src = out.p_y;
+                {
+                    float er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
+                    if (vr::isnan_(er)) er = 0.f;
+                    if (vr::next1D(sg) < er) { p_src *= er; out.lightID = kSelfEmissionLightID; }
+                    else p_src *= lightPdf * (1 - er);
+                }
+                out.runningSum = p_src == 0.f ? 0.f : 1.f;
+                out.p_y = p_src;
+                {
+                    float p_y;
+                    pathPHat *= Tr;
+                    pathPHat *= density;
+                    const bool emis = out.lightID == kSelfEmissionLightID;
+                    if (emis) p_y = pathPHat * vr::luminance(sigma_a * Le);
+                    else p_y = pathPHat * vr::luminance(sigma_s * Ld * lightPdf);
+                    pathPHat *= vr::luminance(sigma_s) * pdfDir;
+                    if (out.runningSum > 0.f) {
+                        if (!emis && lv && o.lightSamples != 0 && p_y != 0.f) {
+                            // runningSum keeps p_src and p_y the unoccluded target until T is known
+                            flags |= kLpNeedsT;
+                            out.runningSum = out.p_y;
+                            out.p_y = p_y;
+                            lpAppendQuery(L, mi.p, ls.dir, ls.distance, (c * MB + bounce) * N + pid);
+                        } else {
+                            out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+                            if (emis && bounce > 0) {
+                                out.lightID = vr::asint(mi.p.z); out.uv0 = mi.p.x; out.uv1 = mi.p.y;
+                                p_y /= (hitD * hitD);
+                                out.sampledPixel = encodeTag(out.sampledPixel, 1);
+                            }
+                            out.p_y = p_y;
+                        }
+                    }
+                }
+                pathPdf *= pdfDir;
+                if (MB > 1) {
+                    if (bounce < MB - 1) {
+                        ray = Ray{mi.p, wi, 0, kRayTMax};
+                        if (P.useRR && bounce >= 2) {
+                            if (vr::next1D(sg) < albedo.x) pathPdf *= albedo.x;
+                            else hitEmpty = true;
+                        }
+                    }
+                }
+            } else {
+                f3 Le = envEval(ray.d);
+                pathPHat *= Tr;
+                float p_y = pathPHat * vr::luminance(Le);
+                out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+                out.p_y = p_y;
+                hitEmpty = true;
+            }
+        }
+        const float ub = MB > 1 ? vr::next1D(sg) : 0.f;
+        const size_t slot = (size_t)(c * MB + bounce) * N + pid;
+        L.vrecA[slot] = make_float4(out.runningSum, out.p_y, out.uv0, out.uv1);
+        L.vrecB[slot] = make_int4(out.lightID, out.sampledPixel, flags, __float_as_int(ub));
+        if (hitEmpty) { bounce++; break; }
+    }
+    if (bounce < MB) L.vrecB[(size_t)(c * MB + bounce) * N + pid].z = 0;
+    return primaryDepth;
+}
+
+// generate: GenerateFeatures + the candidates of TraceRays, recorded
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    const int W = P.W, H = P.H, N = P.N;
+    const int pid = py * W + px;
+    const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H));
+    const Ray ray{P.camPos, dir, 0.f, kRayTMax};
+    B.featCur[pid] = featureTransmittance(ray, P.initial.visibilityTStepScale);
+    vr::Rng sg = vr::rng_create((uint32_t)px, (uint32_t)py, (uint32_t)(P.numTotalRounds * P.frameCount));
+    const int M = P.initialM;
+    const int rounds = (M + 3) / 4;
+    int c = 0;
+    for (int rd = 0; rd < rounds; rd++) {
+        float hd[4] = {0, 0, 0, 0}, pd[4] = {0, 0, 0, 0}, trs[4] = {0, 0, 0, 0};
+        int rs = rd == rounds - 1 ? (M - 4 * (rounds - 1)) : 4;
+        sampleDistances(ray, sg, P.initial.visibilityUseLinearSampler != 0, P.initial.visibilityMipLevel, rs, hd, pd, trs);
+        for (int s = 0; s < rs; s++, c++) {
+            float depth = initialSampleLP<MB>(P, ray, hd[s], pd[s], trs[s], sg, L, c, pid);
+            float uc = vr::next1D(sg);
+            L.crec[(size_t)c * N + pid] = make_float2(depth, uc);
+        }
+    }
+    L.rng[pid] = make_uint4(sg.s[0], sg.s[1], sg.s[2], sg.s[3]);
+    (void)H;
+}
+
+// select: resample the recorded candidates with the predicted transmittance, then finish
+// TraceRays (p_hat of the winner) and run TemporalReuse as k_initial does
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    const int W = P.W, N = P.N;
+    const int pid = py * W + px;
+    const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, P.H));
+    const Ray ray{P.camPos, dir, 0.f, kRayTMax};
+    vr::Rng sg;
+    {
+        uint4 s = L.rng[pid];
+        sg.s[0] = s.x; sg.s[1] = s.y; sg.s[2] = s.z; sg.s[3] = s.w;
+    }
+    f3 finalEx[4] = {mk3(0.f), mk3(0.f), mk3(0.f), mk3(0.f)};
+    Reservoir fin = newReservoir();
+    for (int c = 0; c < P.initialM; c++) {
+        const float2 cr = L.crec[(size_t)c * N + pid];
+        Reservoir comb = newReservoir();
+        for (int b = 0; b < MB; b++) {
+            const size_t slot = (size_t)(c * MB + b) * N + pid;
+            const int4 rb = L.vrecB[slot];
+            if (!(rb.z & kLpValid)) break;
+            const float4 ra = L.vrecA[slot];
+            Reservoir out = newReservoir();
+            out.M = 1; out.depth = cr.x;
+            out.runningSum = ra.x; out.p_y = ra.y; out.uv0 = ra.z; out.uv1 = ra.w;
+            out.lightID = rb.x; out.sampledPixel = rb.y;
+            if (rb.z & kLpNeedsT) {
+                float p_y = ra.y * L.T[slot];
+                out.runningSum = ra.x == 0.f ? 0.f : p_y / ra.x;
+                out.p_y = p_y;
+            }
+            if (MB > 1) resampleStepU(out, comb, __int_as_float(rb.w));
+            else comb = out;
+        }
+        if (MB > 1) comb.M = 1;
+        bool sel = resampleStepU(comb, fin, cr.y);
+        if (sel && MB > 1) {
+            int mib = decodeBounces(fin.sampledPixel, MB);
+            for (int b = 0; b < mib; b++) {
+                float4 e = L.ex[(size_t)(c * (MB - 1) + b) * N + pid];
+                finalEx[b] = mk3(e.x, e.y, e.z);
+            }
+        }
+    }
+    const int mib0 = decodeBounces(fin.sampledPixel, MB);
+    for (int b = 0; b < mib0; b++) B.cur.extra[(size_t)b * N + pid] = make_float4(finalEx[b].x, finalEx[b].y, finalEx[b].z, 0.f);
+    fin.startPixel = pid;
+    float ph = evalPHat(fin, B.cur.extra, N, ray, sg, P.spatial, MB);
+    if (fin.runningSum > 0.f) {
+        fin.runningSum *= fin.p_y == 0.f ? 0.f : ph / fin.p_y;
+        fin.p_y = ph;
+    }
+    storeRes(B.cur, pid, fin);
+    if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
+}
+
+// training samples of the network: a pixel, a path depth in [0, MB) and a delta-tracked path at
+// mip 0 give a scattering point x (up to 8 attempts); the light sample at x gives the direction; the target is the
+// residual ratio tracking estimate of the transmittance toward the light (unbiased)
+template <int MB>
+__global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const LpBuffers L, uint32_t seed) {
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    if (i >= L.trainCount) return;
+    vr::Rng sg = vr::rng_create((uint32_t)i & 0x3FFFu, (uint32_t)i >> 14, seed);
+    MediumInteraction mi;
+    mi.valid = false;
+    bool ok = false;
+    // up to 8 attempts at a path that scatters (most misses leave the volume's box at once)
+    for (int att = 0; att < 8 && !ok; att++) {
+        const int px = min(P.W - 1, (int)(vr::next1D(sg) * (float)P.W));
+        const int py = min(P.H - 1, (int)(vr::next1D(sg) * (float)P.H));
+        const int depth = min(MB - 1, (int)(vr::next1D(sg) * (float)MB));
+        Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, P.W, P.H)), 0.f, kRayTMax};
+        ok = true;
+        for (int b = 0; b <= depth; b++) {
+            mi.valid = false;
+            deltaTrack(ray, sg, mi, 0);
+            if (!mi.valid) { ok = false; break; }
+            if (b < depth) {
+                f3 wi;
+                float u0 = vr::next1D(sg), u1 = vr::next1D(sg);
+                samplePhase(mi, -ray.d, wi, u0, u1);
+                ray = Ray{mi.p, wi, 0, kRayTMax};
+            }
+        }
+    }
+    LightSample ls;
+    if (ok) {
+        int lid; float u0, u1;
+        ok = sampleLights(mi.p, P.initial.useEnvironmentLights != 0, P.initial.useAnalyticLights != 0, sg, ls, lid, u0, u1);
+    }
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, -1.f, 0.f);
+    if (ok) {
+        Ray sr{mi.p, ls.dir, 0, ls.distance};
+        float t = computeVisibility(sr, sg, 1, 0, true, VR_TRACK_RESIDUAL_RATIO, 1.f);
+        a = make_float4(mi.p.x, mi.p.y, mi.p.z, ls.dir.x);
+        b = make_float4(ls.dir.y, ls.dir.z, ls.distance, t);
+    }
+    L.train[2 * (size_t)i] = a;
+    L.train[2 * (size_t)i + 1] = b;
+}
+
+}  // namespace vrd

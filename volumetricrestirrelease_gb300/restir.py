@@ -184,10 +184,52 @@ class VolumetricReSTIR:
         ms = (C.c_float * 4)()
         n = C.c_int32()
         self._check(self._lib.vr_kernel_time_totals(self._h, ms, 4, C.byref(n), 1 if reset else 0))
-        return list(ms[:2]), n.value
+        return list(ms[:3]), n.value
 
     def last_launch_count(self):
         return self._lib.vr_last_launch_count(self._h)
+
+    # ---- learned target (transmittance network) ----
+    def net_params(self):
+        out = np.zeros(capi.NET_PARAMS, np.float32)
+        self._check(self._lib.vr_net_get_params(self._h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
+    def set_net_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == capi.NET_PARAMS
+        self._check(self._lib.vr_net_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def net_infer(self, queries_ptr, n, out_ptr, stream=0):
+        self._check(self._lib.vr_net_infer(self._h, C.c_void_p(queries_ptr), n, C.c_void_p(out_ptr), C.c_void_p(stream)))
+
+    def net_gradients(self, samples_ptr, n):
+        g = np.zeros(capi.NET_PARAMS, np.float32)
+        loss = C.c_float()
+        self._check(self._lib.vr_net_gradients(self._h, C.c_void_p(samples_ptr), n, g.ctypes.data_as(C.POINTER(C.c_float)),
+                                               C.byref(loss)))
+        return loss.value, g
+
+    def net_train_step(self, samples_ptr, n):
+        loss = C.c_float()
+        self._check(self._lib.vr_net_train_step(self._h, C.c_void_p(samples_ptr), n, C.byref(loss)))
+        return loss.value
+
+    def net_box(self):
+        out = np.zeros(6, np.float32)
+        cnt = C.c_int64()
+        self._check(self._lib.vr_export_learned(self._h, 4, out.ctypes.data_as(C.c_void_p), out.nbytes, C.byref(cnt)))
+        return out[:3].copy(), out[3:].copy()
+
+    def export_learned(self, which):
+        """0: T per vertex slot, 1: query list (n, 8), 2: training samples (n, 8), 3: step losses."""
+        cnt = C.c_int64()
+        self._check(self._lib.vr_export_learned(self._h, which, None, 0, C.byref(cnt)))
+        n = cnt.value * (8 if which in (1, 2) else 1)
+        out = np.zeros(max(n, 1), np.float32)
+        self._check(self._lib.vr_export_learned(self._h, which, out.ctypes.data_as(C.c_void_p), out.nbytes, C.byref(cnt)))
+        out = out[:n]
+        return out.reshape(-1, 8) if which in (1, 2) else out
 
     def _check(self, r):
         if r != capi.VR_OK:
