@@ -117,6 +117,7 @@ typedef struct vr_options {
     float mLearnedLearningRate;                 /* 1e-3 */
     float mLearnedTFloor;                       /* 0.02: lower clamp of the predicted transmittance */
     uint32_t mLearnedSeed;                      /* 1: weight initialisation and training streams */
+    uint32_t mLearnedTargetMethod;              /* VR_TRACK_RAY_MARCHING: estimator of the training targets (mip 0) */
 } vr_options;
 
 /* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */

@@ -1253,8 +1253,9 @@ static float predict(float o, float floor_) {
     return t > 1.f ? 1.f : t;
 }
 
-// gradient of mean((exp(o) - target)^2) in the training kernel's order: per chunk of 128
-// samples the sums run over the samples in order, then the chunk sums in chunk order
+// gradient of mean((exp(o) - target)^2) with the training kernel's numerics: BF16 weights,
+// activations and dZ, FP32 sums (per chunk of 128 samples in sample order, then chunk sums in
+// chunk order; the tensor core's own order inside the products differs)
 static void gradients(const float* P, const float* samples, int n, const float bmin[3], const float binv[3], float* grad, float* loss) {
     const float invB = 1.f / (float)n;
     std::vector<float> tot(kParams, 0.f), part(kParams);
@@ -1313,7 +1314,8 @@ static void gradients(const float* P, const float* samples, int n, const float b
             for (int t = 0; t < 128; ++t) {
                 float* dz = &dzs[(size_t)t * 64];
                 float* dh = &dhs[(size_t)t * 64];
-                for (int m = 0; m < kHid; ++m) dz[m] = act[(size_t)t * 320 + (l + 1) * 64 + m] > 0.f ? dh[m] : 0.f;
+                // dZ enters both products of the layer rounded to BF16 (tensor-core operands)
+                for (int m = 0; m < kHid; ++m) dz[m] = rb(act[(size_t)t * 320 + (l + 1) * 64 + m] > 0.f ? dh[m] : 0.f);
                 if (l > 0)
                     for (int k = 0; k < kHid; ++k) {
                         float acc = 0.f;
@@ -1887,9 +1889,14 @@ struct Oracle {
         if (ll) loopLimit = true;
     }
 
-    // training samples of the network for this frame (stream seed as the product derives it)
-    void passTrainGenLP(Ctx& c, const CamFrame& cam) {
-        const int S = opts.mLearnedTrainSamples, mb = c.maxBounces;
+    // training samples of the network, drawn from this frame's queries: a pixel and a starting
+    // slot from the sample's own stream, the first slot of the pixel (cyclically) that holds a
+    // query (up to 4 pixels tried), and a full-resolution transmittance estimate of its shadow
+    // ray as the target
+    void passTrainGenLP(Ctx& c) {
+        const int S = opts.mLearnedTrainSamples;
+        const int numSlots = opts.mInitialM * c.maxBounces;
+        const int N = W * H;
         lpTrain.assign((size_t)std::max(S, 0) * 8, 0.f);
         const uint32_t seed = 0x80000000u | ((opts.mLearnedSeed * 0x9E3779B9u + (uint32_t)frameCount) & 0x7FFFFFFFu);
         const int rows = (S + 255) / 256;
@@ -1901,38 +1908,24 @@ struct Oracle {
             for (int r; (r = next.fetch_add(1)) < rows;) {
                 for (int i = r * 256; i < std::min(S, r * 256 + 256); ++i) {
                     Rng sg = rng_create((uint32_t)i & 0x3FFFu, (uint32_t)i >> 14, seed);
-                    MediumInteraction mi;
-                    mi.isValid = false;
-                    bool ok = false;
-                    for (int att = 0; att < 8 && !ok; att++) {
-                        int px = std::min(W - 1, (int)(next1D(sg) * (float)W));
-                        int py = std::min(H - 1, (int)(next1D(sg) * (float)H));
-                        int depth = std::min(mb - 1, (int)(next1D(sg) * (float)mb));
-                        Ray ray{cam.posW, normalize(rayDirPinhole(cam, px, py, W, H)), 0.f, kRayTMax};
-                        ok = true;
-                        for (int b = 0; b <= depth; b++) {
-                            mi.isValid = false;
-                            SampleMediumSuperVoxelGeneric(sc, ray, sg, mi, 0, cl.loopLimit);
-                            if (!mi.isValid) { ok = false; break; }
-                            if (b < depth) {
-                                f3 wi;
-                                float u0 = next1D(sg), u1 = next1D(sg);
-                                Sample_p(mi, -ray.dir, wi, u0, u1);
-                                ray = Ray{mi.p, wi, 0, kRayTMax};
-                            }
+                    long slot = -1;
+                    for (int att = 0; att < 4 && slot < 0; ++att) {
+                        const int pid = std::min(N - 1, (int)(next1D(sg) * (float)N));
+                        const int j0 = std::min(numSlots - 1, (int)(next1D(sg) * (float)numSlots));
+                        for (int k = 0; k < numSlots; ++k) {
+                            int j = j0 + k;
+                            if (j >= numSlots) j -= numSlots;
+                            const long s = (long)j * N + pid;
+                            if (lpQueries[(size_t)s * 8 + 6] >= 0.f) { slot = s; break; }
                         }
                     }
-                    SceneLightSample ls;
-                    if (ok) {
-                        int idx; float uv[2];
-                        ok = sampleSceneLights(sc, mi.p, c.initial.useEnvironmentLights, c.initial.useAnalyticLights, sg, ls, idx, uv);
-                    }
                     float* o = &lpTrain[(size_t)i * 8];
-                    if (ok) {
-                        Ray sr{mi.p, ls.rayDir, 0, ls.rayDistance};
-                        float t = computeVisibility(sc, sr, sg, 1, 0, true, VR_TRACK_RESIDUAL_RATIO, 1.f);
-                        o[0] = mi.p.x; o[1] = mi.p.y; o[2] = mi.p.z; o[3] = ls.rayDir.x; o[4] = ls.rayDir.y; o[5] = ls.rayDir.z;
-                        o[6] = ls.rayDistance; o[7] = t;
+                    if (slot >= 0) {
+                        const float* q = &lpQueries[(size_t)slot * 8];
+                        Ray sr{mk3(q[0], q[1], q[2]), mk3(q[3], q[4], q[5]), 0, q[6]};
+                        float t = computeVisibility(sc, sr, sg, 1, 0, true, opts.mLearnedTargetMethod, 1.f);
+                        for (int k = 0; k < 7; ++k) o[k] = q[k];
+                        o[7] = t;
                     } else {
                         o[6] = -1.f;
                     }
@@ -2294,8 +2287,8 @@ struct Oracle {
                 if (cl.loopLimit) loopLimit = true;
             });
         } else if (opts.mUseLearnedPHat && (opts.mEnableTemporalReuse || opts.mEnableSpatialReuse)) {
-            if (opts.mLearnedTrainSamples > 0) passTrainGenLP(c, cam);
             passTraceRaysLP(c, cam, numTotalRounds);
+            if (opts.mLearnedTrainSamples > 0) passTrainGenLP(c);
         } else {
             passTraceRays(c, cam, numTotalRounds);
         }

@@ -1,10 +1,11 @@
 """Learned target (transmittance network) on the GPU against the CPU oracle.
 
 Bars:
-  * training step (CUDA cores): loss, gradient and Adam update bit-exact against the oracle's
-    restatement, which sums in the kernel's order;
-  * inference (tcgen05, FP32 accumulation in TMEM): the tensor core's accumulation order is not
-    the oracle's, so T is compared with a tolerance (relative 2e-3 on 99.9 % of the queries);
+  * training step (tcgen05 forward and backward, FP32 accumulation in TMEM): loss and gradient
+    against the oracle's restatement with the same BF16 operands, within the tolerance that the
+    tensor core's accumulation order leaves (relative L2 error 2e-3); the Adam update bit-exact
+    given the kernel's own gradient;
+  * inference (tcgen05): T within relative 2e-3 on 99.9 % of the queries;
   * the split initial pass (generate / infer / select): training samples and the query list
     bit-exact, and -- given the GPU's T -- images, reservoirs and features bit-exact.
 """
@@ -70,7 +71,7 @@ def _same(a, b):
     return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
 
 
-def test_net_gradients_bit_exact(vlib, cuda):
+def test_net_gradients_match_oracle(vlib, cuda):
     from oracle.oracle import net_gradients
     sc, vol, opts, gpu, ora = _ctx(vlib, cuda)
     box = gpu.net_box()
@@ -81,8 +82,14 @@ def test_net_gradients_bit_exact(vlib, cuda):
     loss, g = gpu.net_gradients(d.data_ptr(), len(s))
     lo, go = net_gradients(p, box, s)
     assert np.isfinite(loss) and loss > 0
-    assert _same(loss, lo), (loss, lo)
-    assert _same(g, go), f"{int((g.view(np.uint32) != go.view(np.uint32)).sum())} gradient entries differ"
+    assert abs(loss - lo) <= 1e-3 * lo, (loss, lo)
+    for name, sl in (("hidden 0", slice(0, 4160)), ("hidden 1", slice(4160, 8320)), ("hidden 2", slice(8320, 12480)),
+                     ("hidden 3", slice(12480, 16640)), ("output", slice(16640, NP))):
+        err = np.linalg.norm(g[sl] - go[sl]) / max(np.linalg.norm(go[sl]), 1e-30)
+        assert err < 2e-3, (name, err)
+    # repeated evaluation is bit-identical (no atomics)
+    loss2, g2 = gpu.net_gradients(d.data_ptr(), len(s))
+    assert _same(g, g2) and loss == loss2
 
 
 def test_net_adam_step_bit_exact(vlib, cuda):
@@ -93,9 +100,9 @@ def test_net_adam_step_bit_exact(vlib, cuda):
     gpu.set_net_params(p)
     s = _samples(6, 512, box)
     d = cuda.from_numpy(s).cuda()
+    _, g = gpu.net_gradients(d.data_ptr(), len(s))
     gpu.net_train_step(d.data_ptr(), len(s))
     p1 = gpu.net_params()
-    _, g = net_gradients(p, box, s)
     f = np.float32
     m = f(0.1) * g
     v = f(0.001) * g * g
@@ -137,6 +144,7 @@ def test_learned_frames_match_oracle(vlib, cuda):
     losses = []
     for f in range(3):
         cam = sc.camera(f)
+        params, box = gpu.net_params(), gpu.net_box()     # the weights this frame infers with
         gpu.execute(cam, out.data_ptr())
         cuda.cuda.synchronize()
         img = out.cpu().numpy()
@@ -144,7 +152,7 @@ def test_learned_frames_match_oracle(vlib, cuda):
         qg = gpu.export_learned(1)
         tg = gpu.export_learned(2)
         losses.append(gpu.export_learned(3))
-        params, box = gpu.net_params(), gpu.net_box()
+        assert not _same(params, gpu.net_params()), "the frame's training step did not change the weights"
         ora.set_lp_T(T)
         ref = ora.render_frame(cam)
         # training samples of the frame

@@ -38,8 +38,8 @@ VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 #undef VR_DECL
 // the network kernels (lp.cu)
 cudaError_t net_setup();
-void launch_net_infer(const vrd::NetView&, const float4*, int, const int*, float*, int, int*, int, cudaStream_t);
-void launch_net_train(const vrd::NetView&, const float4*, int, float*, float*, cudaStream_t);
+void launch_net_infer(const vrd::NetView&, const float4*, int, const int*, float*, const int*, int*, int, cudaStream_t);
+void launch_net_train(const vrd::NetView&, const float4*, int, float*, float*, int*, cudaStream_t);
 void launch_net_reduce_adam(const float*, int, const float*, float*, float*, float*, float*, float*, uint16_t*, float*, float, float, float, int,
                             cudaStream_t);
 void launch_net_pack(const float*, uint16_t*, float*, cudaStream_t);
@@ -298,7 +298,7 @@ static int alloc_buffers(vr_context* c) {
 // ---- learned target: network state and the buffers of the split initial pass ----
 static void free_lp(vr_context* c) {
     cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.ex); cudaFree(c->lp.T);
-    cudaFree(c->lp.query); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
+    cudaFree(c->lp.query); cudaFree(c->lp.qlist); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
     c->lp = vrd::LpBuffers{};
     c->lpSlots = 0; c->lpM = 0; c->lpMB = 0;
 }
@@ -404,10 +404,11 @@ static int lp_alloc(vr_context* c) {
         c->lp.ex = dalloc<float4>((size_t)M * std::max(MB - 1, 1) * N);
         c->lp.T = dalloc<float>(slots);
         c->lp.query = dalloc<float4>(2 * slots);
+        c->lp.qlist = dalloc<int>(slots);
         c->lp.qcount = dalloc<int>(1);
         c->lp.rng = dalloc<uint4>(N);
         c->lp.train = dalloc<float4>(2 * (size_t)std::max(S, 1));
-        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qcount || !c->lp.rng || !c->lp.train) {
+        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train) {
             free_lp(c);
             c->err = "out of device memory (learned-target buffers)";
             return VR_ERR_OOM;
@@ -415,6 +416,7 @@ static int lp_alloc(vr_context* c) {
         cudaMemset(c->lp.T, 0, slots * sizeof(float));
         cudaMemset(c->lp.qcount, 0, sizeof(int));
         c->lp.qcapacity = (int)slots;
+        c->lp.numSlots = M * MB;
         c->lp.trainCount = S;
         c->lpSlots = slots; c->lpM = M; c->lpMB = MB;
     }
@@ -449,6 +451,7 @@ static bool options_valid(const vr_options* o, std::string& why) {
         if (o->mLearnedBatch < 1 || o->mLearnedBatch > (1 << 20)) { why = "mLearnedBatch must be in [1, 2^20]"; return false; }
         if (!(o->mLearnedLearningRate >= 0.f) || !(o->mLearnedLearningRate < 1.f)) { why = "mLearnedLearningRate must be in [0, 1)"; return false; }
         if (!(o->mLearnedTFloor > 0.f) || !(o->mLearnedTFloor <= 1.f)) { why = "mLearnedTFloor must be in (0, 1]"; return false; }
+        if (o->mLearnedTargetMethod > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown mLearnedTargetMethod"; return false; }
     }
     return true;
 }
@@ -476,6 +479,16 @@ static bool slots_present(const vr_context* c, std::string& why) {
 
 template <int MB>
 static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st);
+#if !defined(VR_HOST_EMULATION)
+// gathers the records of a slot list (query export)
+__global__ void k_gather_queries(const float4* __restrict__ q, const int* __restrict__ slots, int n, float4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t s = (size_t)slots[i];
+    out[2 * (size_t)i] = q[2 * s];
+    out[2 * (size_t)i + 1] = q[2 * s + 1];
+}
+#endif
 static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st);
 
 extern "C" {
@@ -529,6 +542,7 @@ void vr_options_default(vr_options* o) {
     o->mLearnedLearningRate = 1e-3f;
     o->mLearnedTFloor = 0.02f;
     o->mLearnedSeed = 1;
+    o->mLearnedTargetMethod = VR_TRACK_RAY_MARCHING;
 }
 
 // ---- volumes ----
@@ -987,13 +1001,13 @@ int vr_last_timings(const vr_context* c, float* ms, int32_t max_entries, int32_t
 }
 int32_t vr_last_launch_count(const vr_context* c) { return c ? c->launches : 0; }
 
-// frame events: start, after training, after the initial stage, after the last kernel;
-// totals: 0 initial stage, 1 spatial/final stage, 2 network training
+// frame events: start, after the initial stage, after the spatial/final stage, after the
+// network training (learned target only); totals: 0 initial, 1 spatial/final, 2 training
 static void drain_events(vr_context* c) {
     for (auto& v : c->pendingEv) {
         cudaEventSynchronize(v.back());
         if (v.size() == 4) {
-            const int map[3][3] = {{1, 2, 0}, {2, 3, 1}, {0, 1, 2}};
+            const int map[3][3] = {{0, 1, 0}, {1, 2, 1}, {2, 3, 2}};
             for (auto& m : map) {
                 float t = 0.f;
                 cudaEventElapsedTime(&t, v[m[0]], v[m[1]]);
@@ -1034,7 +1048,7 @@ int vr_net_infer(vr_context* c, const float* q, int32_t n, float* out, void* str
     int r = net_ensure(c, 1);
     if (r) return r;
     if (n == 0) return VR_OK;
-    vrk::launch_net_infer(net_view(c), (const float4*)q, n, nullptr, out, 0, c->status, c->numSMs, (cudaStream_t)stream);
+    vrk::launch_net_infer(net_view(c), (const float4*)q, n, nullptr, out, nullptr, c->status, c->numSMs, (cudaStream_t)stream);
     return check_cuda(c, "network inference");
 }
 static int net_grad_common(vr_context* c, const float* samples, int32_t n, float* loss, bool update, float* grads) {
@@ -1045,7 +1059,7 @@ static int net_grad_common(vr_context* c, const float* samples, int32_t n, float
         lp_train_steps(c, (const float4*)samples, n, 0);
         c->launches -= 2;
     } else {
-        vrk::launch_net_train(net_view(c), (const float4*)samples, n, c->netPart, c->netLossPart, 0);
+        vrk::launch_net_train(net_view(c), (const float4*)samples, n, c->netPart, c->netLossPart, c->status, 0);
         vrk::launch_net_reduce_adam(c->netPart, (n + 127) / 128, c->netLossPart, c->netW, c->netM, c->netV, c->netG, c->netScalar, c->netWbf,
                                     c->netBias, 0.f, 1.f, 1.f, 0, 0);
     }
@@ -1087,7 +1101,20 @@ int vr_export_learned(vr_context* c, int32_t which, void* host, size_t bytes, in
         int qc = 0;
         cudaMemcpy(&qc, c->lp.qcount, sizeof(int), cudaMemcpyDeviceToHost);
         *count = std::min(qc, c->lp.qcapacity);
-        src = c->lp.query; need = (size_t)*count * 32;
+        need = (size_t)*count * 32;
+        if (!host) return VR_OK;
+        if (bytes < need) { c->err = "export buffer too small"; return VR_ERR_INVALID_ARG; }
+        if (!*count) return VR_OK;
+        float4* tmp = dalloc<float4>(2 * (size_t)*count);
+        if (!tmp) { c->err = "out of device memory (export)"; return VR_ERR_OOM; }
+#if !defined(VR_HOST_EMULATION)
+        k_gather_queries<<<(int)((*count + 255) / 256), 256>>>(c->lp.query, c->lp.qlist, (int)*count, tmp);
+#else
+        for (int64_t k = 0; k < *count; ++k) { tmp[2 * k] = c->lp.query[2 * (size_t)c->lp.qlist[k]]; tmp[2 * k + 1] = c->lp.query[2 * (size_t)c->lp.qlist[k] + 1]; }
+#endif
+        cudaMemcpy(host, tmp, need, cudaMemcpyDeviceToHost);
+        cudaFree(tmp);
+        return check_cuda(c, "export");
     } else if (which == 2) { *count = c->lp.trainCount; src = c->lp.train; need = (size_t)c->lp.trainCount * 32; }
     else if (which == 3) { *count = c->lastSteps; src = c->stepLoss; need = (size_t)c->lastSteps * sizeof(float); }
     else return VR_ERR_INVALID_ARG;
@@ -1163,7 +1190,7 @@ static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStre
     const int steps = std::max(1, S / Bt);
     const vrd::NetView nv = net_view(c);
     for (int k = 0; k < steps; ++k) {
-        vrk::launch_net_train(nv, samples + 2 * (size_t)k * Bt, Bt, c->netPart, c->netLossPart, st);
+        vrk::launch_net_train(nv, samples + 2 * (size_t)k * Bt, Bt, c->netPart, c->netLossPart, c->status, st);
         c->adamStep++;
         const float c1 = (float)(1.0 - std::pow(0.9, (double)c->adamStep));
         const float c2 = (float)(1.0 - std::pow(0.999, (double)c->adamStep));
@@ -1188,27 +1215,11 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         frameEv.push_back(e);
     };
     mark();
-    cudaEvent_t afterTrain = nullptr;
     const bool lpOn = lp_active(c);
-    if (lpOn) {
-        if (c->opts.mLearnedTrainSamples > 0) {
-            launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(c->opts.mLearnedSeed, c->frameCount), st);
-            c->launches++;
-            lp_train_steps(c, c->lp.train, c->opts.mLearnedTrainSamples, st);
-        } else {
-            c->lastSteps = 0;
-        }
-        if (c->nev < 10) cudaEventRecord(c->ev[c->nev++], st);
-    }
-    {
-        if (!c->freeEv.empty()) { afterTrain = c->freeEv.back(); c->freeEv.pop_back(); }
-        else cudaEventCreate(&afterTrain);
-        cudaEventRecord(afterTrain, st);
-    }
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
-        vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, 1, c->status, c->numSMs, st);
+        vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
         launch_lp_select<MB>(P, B, c->lp, grid, block, st);
         c->launches += 3;
         c->lpFrameDone = true;
@@ -1253,7 +1264,24 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         mark();
     }
     c->finalBuf = totalRoundId % 2;
-    frameEv.insert(frameEv.begin() + 1, afterTrain);
+    // online training of the network on this frame's own queries (used from the next frame on)
+    if (lpOn) {
+        if (o.mLearnedTrainSamples > 0) {
+            c->lp.targetMethod = o.mLearnedTargetMethod;
+            launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(o.mLearnedSeed, c->frameCount), st);
+            c->launches++;
+            lp_train_steps(c, c->lp.train, o.mLearnedTrainSamples, st);
+        } else {
+            c->lastSteps = 0;
+        }
+        mark();
+    } else {
+        cudaEvent_t e;
+        if (!c->freeEv.empty()) { e = c->freeEv.back(); c->freeEv.pop_back(); }
+        else cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        frameEv.push_back(e);
+    }
     c->pendingEv.push_back(frameEv);
     if (c->pendingEv.size() > 512) drain_events(c);
 }

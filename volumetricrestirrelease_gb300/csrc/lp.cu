@@ -107,8 +107,10 @@ __device__ __forceinline__ void load_query(const float4* q, size_t i, float f[kI
 // next layer's A operand; the output layer (64 -> 1) is a per-thread dot product.
 constexpr int kInferSmem = 4 * 8192 + 16384 + (256 + 64 + 4) * 4 + 64;
 
+// idx == nullptr: query qi is record qi and its T goes to out[qi]; otherwise query qi is record
+// idx[qi] (a slot of the frame's per-slot query array) and its T goes to out[idx[qi]]
 __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __restrict__ q, int n, const int* __restrict__ nptr,
-                                                   float* __restrict__ out, int scatter, int* status) {
+                                                   float* __restrict__ out, const int* __restrict__ idx, int* status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     uint16_t* sW = (uint16_t*)smem;                                     // 4 x (64x64) canonical K-major
     uint16_t* sH = (uint16_t*)(smem + 4 * 8192);                        // 128x64 canonical K-major
@@ -139,9 +141,10 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
     bool ok = true;
     for (int tile = blockIdx.x; tile * 128 < n && ok; tile += gridDim.x) {
         const int qi = tile * 128 + tid;
+        const int rec = qi < n ? (idx ? idx[qi] : qi) : 0;
         {
             float f[kInPad];
-            if (qi < n) load_query(q, (size_t)qi, f, net);
+            if (qi < n) load_query(q, (size_t)rec, f, net);
             else {
 #pragma unroll
                 for (int k = 0; k < kInPad; ++k) f[k] = 0.f;
@@ -205,132 +208,238 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
                 o = acc + *sB4;
             }
         }
-        if (ok && qi < n) {
-            const float t = lpn::predict_from_logit(o, net.floor_);
-            if (scatter) out[__float_as_int(q[2 * (size_t)qi + 1].w)] = t;
-            else out[qi] = t;
-        }
+        if (ok && qi < n) out[rec] = lpn::predict_from_logit(o, net.floor_);
     }
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tb, 64);
 }
 
-// Training step on the CUDA cores: each thread owns one sample (forward, loss, backward); the
-// CTA's gradient over its 128 samples is written to its own row of `partials` (no atomics, so a
-// step is deterministic).  Loss: (T(x, w) - target)^2 averaged over the batch, T = exp(o).
-constexpr int kTrainSmem = 4 * 4096 * 4 + 5 * 64 * 128 * 2 + 128 * 65 * 4 + 320 * 4 + 2 * 128 * 4;
+// Training step on the tensor cores.  One CTA of 128 threads owns a tile of 128 samples, one
+// sample per thread (TMEM lane).  Forward: four 128x64x64 BF16 products (as in inference),
+// keeping every layer's BF16 input transposed in shared memory.  Backward, per hidden layer l
+// from the top: dZ_l = dH ∘ [X_{l+1} > 0] is rounded to BF16 and stored twice, as the A operand
+// of dH_l = dZ_l W_l (128x64x64) and, transposed and padded to 128 rows, as the A operand of
+// dW_l = dZ_l^T X_l (128x64, K = 128 samples); both products accumulate in FP32 in TMEM.  The
+// output layer and the biases are reduced on the CUDA cores.  The CTA writes its gradient to
+// its own row of `partials` (no atomics: a step is deterministic).
+// Loss: mean over the batch of (T - target)^2 with T = exp(o); samples with tmax < 0 add zero.
+namespace ts {
+constexpr int W = 0;               // 4 x 8192: W_l, [64 out][64 in] K-major (forward B operand)
+constexpr int WT = 32768;          // 3 x 8192: W_l^T for l = 1..3, [64 in][64 out] K-major (dH B operand)
+constexpr int X = 57344;           // 16384: layer input, [128 samples][64] K-major (forward A operand)
+constexpr int XT = 73728;          // 4 x 16384: X_l^T, [64][128 samples] K-major (dW B operand)
+constexpr int DZ = 139264;         // 16384: dZ, [128 samples][64] K-major (dH A operand)
+constexpr int DZT = 155648;        // 32768: dZ^T padded, [128 rows, 64..127 zero][128 samples] (dW A operand)
+constexpr int F = 188416;          // floats: biases 256, w4 64, b4 1 (+3), g 128, loss 128
+constexpr int MB = F + (256 + 64 + 4 + 128 + 128) * 4;   // mbarrier, TMEM address
+constexpr int Total = MB + 16;
+}  // namespace ts
+constexpr int kTrainSmem = ts::Total;
+constexpr uint32_t kTmemZ = 0, kTmemH = 64, kTmemW = 128;   // column bases; 512 columns allocated
 
-__global__ void __launch_bounds__(128) k_net_train(NetView net, const float4* __restrict__ samples, int n, float invB,
-                                                   float* __restrict__ partials, float* __restrict__ lossParts) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    float* sW = (float*)smem;                                       // 4 x [64 out][64 in]
-    uint16_t* sH = (uint16_t*)(smem + 4 * 4096 * 4);                // 5 x [64][128] activations (bf16)
-    float* sDZ = (float*)(smem + 4 * 4096 * 4 + 5 * 64 * 128 * 2);  // [128][65]
-    float* sMisc = sDZ + 128 * 65;                                  // biases 256, output weights 64
-    float* sG = sMisc + 320;                                        // per-sample dL/do
-    float* sL = sG + 128;                                           // per-sample loss
-    const int tid = threadIdx.x;
-    for (int i = tid; i < 4 * 4096; i += 128) sW[i] = lpn::bf2f(net.wbf[i]);
-    for (int i = tid; i < 256; i += 128) sMisc[i] = net.bias[i];
-    if (tid < 64) sMisc[256 + tid] = lpn::bf2f(net.wbf[4 * 4096 + tid]);
+__device__ __forceinline__ void st_row_bf16(unsigned char* base, int row, const float* v, int K) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        uint4 u;
+        u.x = (uint32_t)lpn::f2bf(v[8 * c + 0]) | ((uint32_t)lpn::f2bf(v[8 * c + 1]) << 16);
+        u.y = (uint32_t)lpn::f2bf(v[8 * c + 2]) | ((uint32_t)lpn::f2bf(v[8 * c + 3]) << 16);
+        u.z = (uint32_t)lpn::f2bf(v[8 * c + 4]) | ((uint32_t)lpn::f2bf(v[8 * c + 5]) << 16);
+        u.w = (uint32_t)lpn::f2bf(v[8 * c + 6]) | ((uint32_t)lpn::f2bf(v[8 * c + 7]) << 16);
+        *(uint4*)(base + umma::canon_offset(row, 8 * c, K)) = u;
+    }
+}
+// column `col` of a [64 rows][128] K-major tile: v[r] -> element (r, col)
+__device__ __forceinline__ void st_col_bf16(unsigned char* base, int col, const float* v) {
+#pragma unroll
+    for (int r = 0; r < 64; ++r) *(uint16_t*)(base + umma::canon_offset(r, col, 128)) = lpn::f2bf(v[r]);
+}
+
+__device__ __forceinline__ bool train_mma_wait(uint64_t* mbar, uint32_t& phase, int* status) {
+    const bool got = umma::mbar_wait_bounded(mbar, phase, status, 8);
+    phase ^= 1u;
+    const bool ok = __syncthreads_and(got ? 1 : 0) != 0;
+    umma::fence_after_sync();
+    return ok;
+}
+__device__ __forceinline__ void train_issue_sync() {
+    umma::fence_async_shared();
+    umma::fence_before_sync();
     __syncthreads();
+    umma::fence_after_sync();
+}
+
+__global__ void __launch_bounds__(128, 1) k_net_train(NetView net, const float4* __restrict__ samples, int n, float invB,
+                                                      float* __restrict__ partials, float* __restrict__ lossParts, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float* sBias = (float*)(smem + ts::F);
+    float* sW4 = sBias + 256;
+    float* sB4 = sW4 + 64;
+    float* sG = sB4 + 4;
+    float* sL = sG + 128;
+    uint64_t* mbar = (uint64_t*)(smem + ts::MB);
+    uint32_t* tmem_slot = (uint32_t*)(smem + ts::MB + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights (and their transposes) in the canonical K-major layout, zero padding of dZ^T
+    for (int i = tid; i < 4 * 4096; i += 128) {
+        const int l = i >> 12, r = (i >> 6) & 63, k = i & 63;
+        const uint16_t w = net.wbf[i];
+        *(uint16_t*)(smem + ts::W + l * 8192 + umma::canon_offset(r, k, 64)) = w;
+        if (l > 0) *(uint16_t*)(smem + ts::WT + (l - 1) * 8192 + umma::canon_offset(k, r, 64)) = w;
+    }
+    for (int i = tid; i < 16384 / 16; i += 128) *(uint4*)(smem + ts::DZT + 16384 + 16 * i) = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < 256; i += 128) sBias[i] = net.bias[i];
+    if (tid < 64) sW4[tid] = lpn::bf2f(net.wbf[4 * 4096 + tid]);
+    if (tid == 0) *sB4 = net.bias[256];
+    if (warp == 0) umma::tmem_alloc(tmem_slot, 512);
+    if (tid == 0) umma::mbar_init(mbar, 1);
+    train_issue_sync();
+    const uint32_t tb = *tmem_slot;
+    const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
+    const uint32_t id64 = umma::idesc_bf16_f32(128, 64);
+    uint32_t phase = 0;
+    bool ok = true;
+
     const int si = blockIdx.x * 128 + tid;
     bool valid = si < n;
-    float h[kHid];
+    float h[64];
     {
-        float f[kInPad];
-        if (valid) {
-            load_query(samples, (size_t)si, f, net);
+        if (si < n) {
+            load_query(samples, (size_t)si, h, net);
             valid = samples[2 * (size_t)si + 1].z >= 0.f;
         } else {
-            for (int k = 0; k < kInPad; ++k) f[k] = 0.f;
+#pragma unroll
+            for (int k = 0; k < 64; ++k) h[k] = 0.f;
         }
-        for (int k = 0; k < kInPad; ++k) {
-            uint16_t b = lpn::f2bf(f[k]);
-            sH[k * 128 + tid] = b;
-            h[k] = lpn::bf2f(b);
+        st_row_bf16(smem + ts::X, tid, h, 64);
+        st_col_bf16(smem + ts::XT, tid, h);
+    }
+    // forward
+    for (int l = 0; l < 4 && ok; ++l) {
+        train_issue_sync();
+        if (tid == 0) {
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                uint64_t a = umma::make_desc(umma::smem_addr(smem + ts::X) + 256u * s, 128u, 1024u);
+                uint64_t b = umma::make_desc(umma::smem_addr(smem + ts::W + l * 8192) + 256u * s, 128u, 1024u);
+                umma::mma_bf16(tb + kTmemZ, a, b, id64, s > 0 ? 1u : 0u);
+            }
+            umma::commit_to(mbar);
+        }
+        if (!(ok = train_mma_wait(mbar, phase, status))) break;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) umma::tmem_ld16(tb + lane_off + kTmemZ + 16u * c, h + 16 * c);
+#pragma unroll
+        for (int k = 0; k < 64; ++k) {
+            const float a = h[k] + sBias[l * 64 + k];
+            h[k] = lpn::round_bf(a > 0.f ? a : 0.f);
+        }
+        if (l < 3) {
+            st_row_bf16(smem + ts::X, tid, h, 64);
+            st_col_bf16(smem + ts::XT + (l + 1) * 16384, tid, h);
         }
     }
-    for (int l = 0; l < 4; ++l) {
-        const float* W = sW + l * 4096;
-        float hn[kHid];
-        for (int nn = 0; nn < kHid; ++nn) {
-            float acc = 0.f;
-#pragma unroll 16
-            for (int k = 0; k < kInPad; ++k) acc += W[nn * 64 + k] * h[k];
-            float a = acc + sMisc[l * 64 + nn];
-            uint16_t b = lpn::f2bf(a > 0.f ? a : 0.f);
-            sH[((l + 1) * 64 + nn) * 128 + tid] = b;
-            hn[nn] = lpn::bf2f(b);
+    // output layer, loss, dL/do
+    float g = 0.f;
+    if (ok) {
+        float o = 0.f;
+#pragma unroll
+        for (int k = 0; k < 64; ++k) o += h[k] * sW4[k];
+        o += *sB4;
+        float lv = 0.f;
+        if (valid) {
+            const float p = vr::exp_(o);
+            const float d = p - samples[2 * (size_t)si + 1].w;
+            g = 2.f * d * p * invB;
+            lv = d * d * invB;
         }
-        for (int k = 0; k < kHid; ++k) h[k] = hn[k];
+        sG[tid] = g;
+        sL[tid] = lv;
+        st_row_bf16(smem + ts::X, tid, h, 64);      // X_4 (exact: already BF16 values)
     }
-    float o = 0.f;
-    for (int k = 0; k < kHid; ++k) o += h[k] * sMisc[256 + k];
-    o += net.bias[256];
-    float g = 0.f, lv = 0.f;
-    if (valid) {
-        const float p = vr::exp_(o);
-        const float d = p - samples[2 * (size_t)si + 1].w;
-        g = 2.f * d * p * invB;
-        lv = d * d * invB;
-    }
-    sG[tid] = g;
-    sL[tid] = lv;
     float* part = partials + (size_t)blockIdx.x * lpn::kParamsPad;
-    // output layer
-    float dh[kHid];
-    for (int k = 0; k < kHid; ++k) dh[k] = g * sMisc[256 + k];
-    for (int k = 0; k < kHid; ++k) sDZ[tid * 65 + k] = h[k];
     __syncthreads();
-    if (tid < 64) {
-        float acc = 0.f;
-        for (int t = 0; t < 128; ++t) acc += sG[t] * sDZ[t * 65 + tid];
-        part[lpn::kOutW + tid] = acc;
-    } else if (tid == 64) {
-        float acc = 0.f, ls = 0.f;
-        for (int t = 0; t < 128; ++t) { acc += sG[t]; ls += sL[t]; }
-        part[lpn::kOutB] = acc;
-        lossParts[blockIdx.x] = ls;
-    }
-    __syncthreads();
-    for (int l = 3; l >= 0; --l) {
-        const float* W = sW + l * 4096;
-        float dz[kHid];
-        for (int nn = 0; nn < kHid; ++nn) {
-            float hv = lpn::bf2f(sH[((l + 1) * 64 + nn) * 128 + tid]);
-            dz[nn] = hv > 0.f ? dh[nn] : 0.f;
-            sDZ[tid * 65 + nn] = dz[nn];
+    if (ok) {
+        if (tid < 64) {
+            float acc = 0.f;
+            for (int t = 0; t < 128; ++t) acc += sG[t] * lpn::bf2f(*(const uint16_t*)(smem + ts::X + umma::canon_offset(t, tid, 64)));
+            part[lpn::kOutW + tid] = acc;
+        } else if (tid == 64) {
+            float acc = 0.f, ls = 0.f;
+            for (int t = 0; t < 128; ++t) { acc += sG[t]; ls += sL[t]; }
+            part[lpn::kOutB] = acc;
+            lossParts[blockIdx.x] = ls;
         }
+    }
+    // backward through the hidden layers; h holds X_{l+1} of this sample
+    float dz[64];
+#pragma unroll
+    for (int k = 0; k < 64; ++k) dz[k] = h[k] > 0.f ? g * sW4[k] : 0.f;
+    for (int l = 3; l >= 0 && ok; --l) {
+        st_row_bf16(smem + ts::DZ, tid, dz, 64);
+        // column tid of dZ^T (rows 0..63)
+#pragma unroll
+        for (int r = 0; r < 64; ++r) *(uint16_t*)(smem + ts::DZT + umma::canon_offset(r, tid, 128)) = lpn::f2bf(dz[r]);
+        train_issue_sync();
+        if (tid == 0) {
+            if (l > 0) {
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    uint64_t a = umma::make_desc(umma::smem_addr(smem + ts::DZ) + 256u * s, 128u, 1024u);
+                    uint64_t b = umma::make_desc(umma::smem_addr(smem + ts::WT + (l - 1) * 8192) + 256u * s, 128u, 1024u);
+                    umma::mma_bf16(tb + kTmemH, a, b, id64, s > 0 ? 1u : 0u);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                uint64_t a = umma::make_desc(umma::smem_addr(smem + ts::DZT) + 256u * s, 128u, 2048u);
+                uint64_t b = umma::make_desc(umma::smem_addr(smem + ts::XT + l * 16384) + 256u * s, 128u, 2048u);
+                umma::mma_bf16(tb + kTmemW + 64u * l, a, b, id64, s > 0 ? 1u : 0u);
+            }
+            umma::commit_to(mbar);
+        }
+        // bias gradient of layer l from the BF16 dZ^T rows (read while the products run)
+        if (tid < 64) {
+            float acc = 0.f;
+            for (int t0 = 0; t0 < 128; t0 += 8) {
+                const uint4 u = *(const uint4*)(smem + ts::DZT + umma::canon_offset(tid, t0, 128));
+                const uint32_t w4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    acc += lpn::bf2f((uint16_t)(w4[j] & 0xFFFFu));
+                    acc += lpn::bf2f((uint16_t)(w4[j] >> 16));
+                }
+            }
+            part[lpn::b_off(l) + tid] = acc;
+        }
+        if (!(ok = train_mma_wait(mbar, phase, status))) break;
         if (l > 0) {
-            for (int k = 0; k < kHid; ++k) {
-                float acc = 0.f;
-#pragma unroll 16
-                for (int nn = 0; nn < kHid; ++nn) acc += W[nn * 64 + k] * dz[nn];
-                dh[k] = acc;
+            float dh[64];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) umma::tmem_ld16(tb + lane_off + kTmemH + 16u * c, dh + 16 * c);
+            // ReLU mask from this sample's input of layer l (column tid of X_l^T)
+#pragma unroll
+            for (int k = 0; k < 64; ++k) {
+                const float xv = lpn::bf2f(*(const uint16_t*)(smem + ts::XT + l * 16384 + umma::canon_offset(k, tid, 128)));
+                dz[k] = xv > 0.f ? dh[k] : 0.f;
             }
         }
-        __syncthreads();
-        // dW[nn][k] = sum_t dz[t][nn] * h_l[t][k]: thread -> row nn = tid / 2, half of the k range
-        {
-            const int nn = tid >> 1, k0 = (tid & 1) * 32;
-            float acc[32], accb = 0.f;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) acc[j] = 0.f;
-            for (int t = 0; t < 128; ++t) {
-                const float d = sDZ[t * 65 + nn];
-                accb += d;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) acc[j] += d * lpn::bf2f(sH[(l * 64 + k0 + j) * 128 + t]);
-            }
-            float* gw = part + lpn::w_off(l) + nn * 64 + k0;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) gw[j] = acc[j];
-            if ((tid & 1) == 0) part[lpn::b_off(l) + nn] = accb;
-        }
-        __syncthreads();
     }
+    // weight gradients: TMEM lanes 0..63 (warps 0 and 1) hold the rows of dW_l
+    if (ok && warp < 2) {
+        const int r = tid;
+        for (int l = 0; l < 4; ++l) {
+            float v[64];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) umma::tmem_ld16(tb + lane_off + kTmemW + 64u * l + 16u * c, v + 16 * c);
+            float* gw = part + lpn::w_off(l) + r * 64;
+#pragma unroll
+            for (int k = 0; k < 64; k += 4) *(float4*)(gw + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tb, 512);
 }
 
 __device__ __forceinline__ void scatter_param(int i, float wi, uint16_t* wbf, float* bias) {
@@ -389,16 +498,16 @@ cudaError_t net_setup() {
 }
 
 // grid: persistent, 4 CTAs per SM (TMEM: 4 x 64 columns)
-void launch_net_infer(const vrd::NetView& net, const float4* q, int n, const int* nptr, float* out, int scatter, int* status, int numSMs,
+void launch_net_infer(const vrd::NetView& net, const float4* q, int n, const int* nptr, float* out, const int* idx, int* status, int numSMs,
                       cudaStream_t st) {
     int tiles = (n + 127) / 128;
     int grid = std::max(1, std::min(tiles, numSMs * 4));
-    lpk::k_net_infer<<<grid, 128, lpk::kInferSmem, st>>>(net, q, n, nptr, out, scatter, status);
+    lpk::k_net_infer<<<grid, 128, lpk::kInferSmem, st>>>(net, q, n, nptr, out, idx, status);
 }
 
-void launch_net_train(const vrd::NetView& net, const float4* samples, int n, float* partials, float* lossParts, cudaStream_t st) {
+void launch_net_train(const vrd::NetView& net, const float4* samples, int n, float* partials, float* lossParts, int* status, cudaStream_t st) {
     int grid = (n + 127) / 128;
-    lpk::k_net_train<<<grid, 128, lpk::kTrainSmem, st>>>(net, samples, n, 1.f / (float)n, partials, lossParts);
+    lpk::k_net_train<<<grid, 128, lpk::kTrainSmem, st>>>(net, samples, n, 1.f / (float)n, partials, lossParts, status);
 }
 
 void launch_net_reduce_adam(const float* partials, int parts, const float* lossParts, float* w, float* m, float* v, float* grads, float* loss,

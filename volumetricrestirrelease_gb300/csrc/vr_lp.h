@@ -7,7 +7,7 @@
 //              light visibility of each next-event estimate is not marched; the vertex's
 //              reservoir fields, its resampling uniform and (where the target needs it) a
 //              transmittance query (x, w, tmax, slot) are written out;
-//   infer    : the network predicts T for the compacted query list;
+//   infer    : the network predicts T for the compacted list of query slots;
 //   select   : the recorded candidates are resampled with p_hat = p_hat_unoccluded * T, then the
 //              pass continues as the plain one (p_hat of the winner, temporal reuse).
 // The random stream of a pixel does not depend on T: the resampling uniforms are drawn at
@@ -36,12 +36,15 @@ struct LpBuffers {
     float2* crec;      // [M][N]: depth, candidate resampling uniform
     float4* ex;        // [M * (MB - 1)][N]: encoded direction / distance of each indirect vertex
     float* T;          // [M * MB][N]: predicted transmittance of the vertices with kLpNeedsT
-    float4* query;     // [capacity][2]: (x, y, z, wx), (wy, wz, tmax, slot as int bits)
+    float4* query;     // [M * MB][N][2]: the query of each slot with kLpNeedsT: (x, y, z, wx), (wy, wz, tmax, slot bits)
+    int* qlist;        // compacted list of the slots that hold a query (in arbitrary order)
     int* qcount;
     int qcapacity;
     uint4* rng;        // [N]: the pixel's random state after generation
     float4* train;     // [S][2]: (x, y, z, wx), (wy, wz, tmax or -1 when invalid, target)
     int trainCount;
+    int numSlots;      // M * MB
+    uint32_t targetMethod;   // transmittance estimator of the training targets (mip 0, trilinear)
 };
 
 }  // namespace vrd

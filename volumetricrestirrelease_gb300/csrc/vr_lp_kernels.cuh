@@ -23,8 +23,11 @@ __device__ __forceinline__ bool resampleStepU(const Reservoir& r, Reservoir& s, 
     return sel;
 }
 
-// appends one transmittance query; the threads that reach this point together share one atomic
+// stores the query of a slot and appends the slot to the compacted list; the threads that reach
+// this point together share one atomic
 __device__ __forceinline__ void lpAppendQuery(const LpBuffers& L, f3 x, f3 w, float tmax, int slot) {
+    L.query[2 * (size_t)slot] = make_float4(x.x, x.y, x.z, w.x);
+    L.query[2 * (size_t)slot + 1] = make_float4(w.y, w.z, tmax, __int_as_float(slot));
     const unsigned m = __activemask();
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
@@ -34,8 +37,7 @@ __device__ __forceinline__ void lpAppendQuery(const LpBuffers& L, f3 x, f3 w, fl
     base = __shfl_sync(m, base, leader);
     const int idx = base + rank;
     if (idx < L.qcapacity) {
-        L.query[2 * (size_t)idx] = make_float4(x.x, x.y, x.z, w.x);
-        L.query[2 * (size_t)idx + 1] = make_float4(w.y, w.z, tmax, __int_as_float(slot));
+        L.qlist[idx] = slot;
     } else if (c_scene.status) {
         atomicOr(c_scene.status, 2);
     }
@@ -263,47 +265,34 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const Fr
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
 
-// training samples of the network: a pixel, a path depth in [0, MB) and a delta-tracked path at
-// mip 0 give a scattering point x (up to 8 attempts); the light sample at x gives the direction; the target is the
-// residual ratio tracking estimate of the transmittance toward the light (unbiased)
+// training samples of the network, drawn from the queries the frame's candidates made: sample i
+// picks a pixel and a starting slot from its own stream and takes the first slot of that pixel
+// (cyclically from the start) that holds a query, with up to 4 pixels tried; the target is a full-resolution (mip 0,
+// trilinear) estimate of the transmittance of the query's shadow ray, by ray marching (default) or
+// by (residual) ratio tracking.  A sample that found no query is invalid (tmax = -1).
 template <int MB>
 __global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const LpBuffers L, uint32_t seed) {
     const int i = blockIdx.x * 128 + threadIdx.x;
     if (i >= L.trainCount) return;
+    const int N = P.N, S = L.numSlots;
     vr::Rng sg = vr::rng_create((uint32_t)i & 0x3FFFu, (uint32_t)i >> 14, seed);
-    MediumInteraction mi;
-    mi.valid = false;
-    bool ok = false;
-    // up to 8 attempts at a path that scatters (most misses leave the volume's box at once)
-    for (int att = 0; att < 8 && !ok; att++) {
-        const int px = min(P.W - 1, (int)(vr::next1D(sg) * (float)P.W));
-        const int py = min(P.H - 1, (int)(vr::next1D(sg) * (float)P.H));
-        const int depth = min(MB - 1, (int)(vr::next1D(sg) * (float)MB));
-        Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, P.W, P.H)), 0.f, kRayTMax};
-        ok = true;
-        for (int b = 0; b <= depth; b++) {
-            mi.valid = false;
-            deltaTrack(ray, sg, mi, 0);
-            if (!mi.valid) { ok = false; break; }
-            if (b < depth) {
-                f3 wi;
-                float u0 = vr::next1D(sg), u1 = vr::next1D(sg);
-                samplePhase(mi, -ray.d, wi, u0, u1);
-                ray = Ray{mi.p, wi, 0, kRayTMax};
-            }
+    int slot = -1;
+    for (int att = 0; att < 4 && slot < 0; ++att) {
+        const int pid = min(N - 1, (int)(vr::next1D(sg) * (float)N));
+        const int j0 = min(S - 1, (int)(vr::next1D(sg) * (float)S));
+        for (int k = 0; k < S; ++k) {
+            int j = j0 + k;
+            if (j >= S) j -= S;
+            if (reinterpret_cast<const int*>(L.vrecB + (size_t)j * N + pid)[2] & kLpNeedsT) { slot = j * N + pid; break; }
         }
     }
-    LightSample ls;
-    if (ok) {
-        int lid; float u0, u1;
-        ok = sampleLights(mi.p, P.initial.useEnvironmentLights != 0, P.initial.useAnalyticLights != 0, sg, ls, lid, u0, u1);
-    }
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = make_float4(0.f, 0.f, -1.f, 0.f);
-    if (ok) {
-        Ray sr{mi.p, ls.dir, 0, ls.distance};
-        float t = computeVisibility(sr, sg, 1, 0, true, VR_TRACK_RESIDUAL_RATIO, 1.f);
-        a = make_float4(mi.p.x, mi.p.y, mi.p.z, ls.dir.x);
-        b = make_float4(ls.dir.y, ls.dir.z, ls.distance, t);
+    if (slot >= 0) {
+        a = L.query[2 * (size_t)slot];
+        const float4 q1 = L.query[2 * (size_t)slot + 1];
+        Ray sr{mk3(a.x, a.y, a.z), mk3(a.w, q1.x, q1.y), 0, q1.z};
+        const float t = computeVisibility(sr, sg, 1, 0, true, L.targetMethod, 1.f);
+        b = make_float4(q1.x, q1.y, q1.z, t);
     }
     L.train[2 * (size_t)i] = a;
     L.train[2 * (size_t)i + 1] = b;
