@@ -1,9 +1,17 @@
 """Benchmark of the Volumetric ReSTIR frame loop on GB300.
 
-Workload (one "step" = one frame of the plain method): 1920x1080, 512^3 sparse fBm cloud in
-8^3 bricks with a 4-level conservative pyramid, max path length 3, 32 initial candidates,
-temporal reuse + 3 spatial neighbours, 16 point lights + procedural sky, camera orbiting
-0.5 deg per frame.  Synthetic data (the reference's .vbx clouds are not available).
+Workload (one "step" = one frame): 1920x1080, 512^3 sparse fBm cloud in 8^3 bricks with a
+4-level conservative pyramid, max path length 3, temporal reuse + 3 spatial neighbours, 16 point
+lights + procedural sky, camera orbiting 0.5 deg per frame.  Synthetic data (the reference's .vbx
+clouds are not available).
+
+Metric: 1080p frames/s of the learned-target form (transmittance MLP in the initial RIS target,
+FP16 bricks) at a relMSE against the FP64 path-traced reference matched to the plain form's
+(FP32 bricks, 32 candidates).  The match is made in the run: the relMSE of each form is measured
+at 480x270 on a static camera over frames 16..127 against a 1024-spp FP64 reference rendered on
+the GPU, and the learned form takes the smallest candidate count in {32, 36, 40, 48} whose relMSE
+is not above the plain form's by more than two standard errors of the difference (block means
+of 16 frames).  The plain form's frames/s is reported beside it.
 
 Output: one JSON line (rank 0).  `value` = frames/s with every input resident in HBM
 (vr_render_frame into a device buffer, CUDA events on the launching stream); `e2e` = the same
@@ -33,7 +41,10 @@ ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "1080p frames/s at matched relMSE vs FP64 ref; learned-p-hat vs plain, 1 GB300"
-WORKLOAD = "plain ReSTIR frame, 1920x1080, 512^3 sparse fBm (8^3 bricks, 4-level conservative mips), max path length 3, M=32, temporal + 3 spatial neighbours, 16 point lights + 512x256 sky, orbiting camera"
+WORKLOAD = ("learned-p-hat + FP16-brick ReSTIR frame, 1920x1080, 512^3 sparse fBm (8^3 bricks, 4-level conservative mips), "
+            "max path length 3, temporal + 3 spatial neighbours, 16 point lights + 512x256 sky, orbiting camera; "
+            "candidate count matched to the plain form's relMSE (plain: FP32 bricks, M=32)")
+LEARNED_M = (32, 36, 40, 48)
 
 
 def _peaks():
@@ -42,6 +53,15 @@ def _peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def _bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured (burst)"
+    return 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -98,40 +118,129 @@ def _dist():
     return ws, rank
 
 
-def _scene(args):
+def _scene(args, fp16=False, static=False, width=None, height=None):
     from volumetricrestirrelease_gb300 import scenes
-    return scenes.full(width=args.width, height=args.height)
+    sc = scenes.full(width=width or args.width, height=height or args.height, fp16=fp16)
+    if static:
+        sc.orbit_deg_per_frame = 0.0
+    return sc
 
 
-def _options(lib, sc):
+def _options(lib, sc, learned=False, M=None):
     from volumetricrestirrelease_gb300 import capi
     o = capi.default_options(lib)
     for k, v in sc.options.items():
         setattr(o, k, v)
+    if learned:
+        o.mUseLearnedPHat = 1
+    if M:
+        o.mInitialM = M
     return o
 
 
 def stream_bytes_per_pixel(mb, K):
-    """Algorithmic SoA stream bytes per pixel of each fused kernel (reservoir a/b = 32 B, one
-    extra-bounce record = 16 B, feature = 4 B, output pixel = 16 B)."""
+    """Algorithmic SoA stream bytes per pixel of the plain form's fused kernels (reservoir a/b =
+    32 B, one extra-bounce record = 16 B, feature = 4 B, output pixel = 16 B)."""
     ex = 16 * (mb - 1)
     initial = 4 + 32 + ex + (32 + ex + 4)           # features + reservoir + suffix written; history tap + prev feature read
     spatial = K * 32 + 4 + (32 + ex) + (32 + ex) + 16   # K taps + centre feature; output + history; image
     return {"k_initial": initial, "k_spatial": spatial}
 
 
-def cpu_sample(args, threads, frames=2, scale_w=4, scale_h=4):
-    """Times the oracle (CPU restatement) on a crop-free reduced-resolution run of the same
-    scene: frame 0 untimed, frame 1 timed (temporal + spatial), scaled by pixel count."""
+def generate_stream_bytes_per_pixel(M, vertices_px, queries_px):
+    """k_lp_generate's algorithmic stream bytes per pixel: feature 4 B, random state 16 B,
+    candidate record 8 B per candidate, vertex record 32 B per vertex, suffix record 16 B per
+    indirect vertex, query 32 B + slot index 4 B per query."""
+    return 4 + 16 + 8 * M + 32 * vertices_px + 16 * max(vertices_px - M, 0) + 36 * queries_px
+
+
+NET_FLOP_PER_QUERY = 4 * 2 * 64 * 64 + 2 * 64      # four 64x64 layers and the output dot product
+
+
+def _relmse(img, ref):
+    return float(np.mean((img[..., :3].astype(np.float64) - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=1024, block=16):
+    """relMSE of each form against an FP64 path-traced reference at QWxQH, static camera,
+    averaged over frames first..frames-1, with the standard error of that mean from the means of
+    blocks of `block` consecutive frames (consecutive frames are correlated through temporal
+    reuse).  forms: {name: (fp16, learned, M)} -> {name: (mean, standard error)}."""
+    import torch
+    from volumetricrestirrelease_gb300.restir import VolumetricReSTIR
+    sc = _scene(args, static=True, width=QW, height=QH)
+    rd = VolumetricReSTIR(QW, QH, _options(lib, sc).as_dict(), lib=lib)
+    rd.setScene(vols[False], sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+    acc = torch.zeros((QH, QW, 3), device="cuda", dtype=torch.float64)
+    for f0 in range(0, spp, 64):
+        rd.render_reference(sc.camera(0), acc.data_ptr(), f0, min(64, spp - f0))
+    torch.cuda.synchronize()
+    ref = (acc / spp).cpu().numpy()
+    del rd
+    out = torch.empty((QH, QW, 4), device="cuda")
+    res = {}
+    for name, (fp16, learned, M) in forms.items():
+        scf = _scene(args, fp16=fp16, static=True, width=QW, height=QH)
+        rd = VolumetricReSTIR(QW, QH, _options(lib, scf, learned, M).as_dict(), lib=lib)
+        rd.setScene(vols[fp16], scf.medium, scf.lights, scf.env_rgb, scf.env_scale)
+        errs = []
+        for f in range(frames):
+            rd.execute(scf.camera(f), out.data_ptr())
+            if f >= first:
+                torch.cuda.synchronize()
+                errs.append(_relmse(out.cpu().numpy(), ref))
+        e = np.asarray(errs)
+        bm = e[: len(e) // block * block].reshape(-1, block).mean(1)
+        res[name] = (float(e.mean()), float(bm.std(ddof=1) / np.sqrt(len(bm))))
+        del rd
+    return res, {"resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
+                 "reference": f"{spp} spp FP64 path tracer on the GPU", "relmse": "mean over pixels and RGB of (x-r)^2/(r^2+0.01)",
+                 "standard_error": f"from the means of blocks of {block} frames"}
+
+
+def _time_frames(rd, sc, out, sptr, warmup, steps, first=0, clock_index=None, barrier=lambda: None):
+    import torch
+    for f in range(first, first + warmup):
+        rd.execute(sc.camera(f), out.data_ptr(), stream=sptr)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    rd.kernel_time_totals(reset=True)
+    launches = 0
+    clk = ClockSampler(clock_index) if clock_index is not None else None
+    if clk:
+        clk.__enter__()
+    try:
+        e0.record(stream)
+        for f in range(first + warmup, first + warmup + steps):
+            rd.execute(sc.camera(f), out.data_ptr(), stream=sptr)
+            launches += rd.last_launch_count()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    finally:
+        if clk:
+            clk.__exit__()
+    barrier()
+    tot, nfr = rd.kernel_time_totals(reset=True)
+    ms = e0.elapsed_time(e1)
+    return ms, [t / max(nfr, 1) for t in tot], launches, (clk.summary() if clk else None)
+
+
+def cpu_sample(args, threads, frames=2, scale_w=4, scale_h=4, learned=None):
+    """Times the oracle (CPU restatement) on a reduced-resolution run of the plain form of the
+    same scene: frame 0 untimed, frame 1 timed (temporal + spatial), scaled by pixel count.
+    With learned = (M, params, box) it also runs the learned form (CPU network) for the
+    per-pixel voxel reads, vertex records and queries of the generate kernel."""
     from oracle import oracle as O
     from volumetricrestirrelease_gb300 import capi
     from volumetricrestirrelease_gb300.restir import Volume
     lib = capi.load()
     W, H = args.width // scale_w, args.height // scale_h
-    sc = _scene(args)
+    sc = _scene(args, width=W, height=H)
     vol = Volume.procedural(sc.volume, lib=lib)
-    opts = _options(lib, sc)
-    ora = O.Oracle(W, H, opts, threads=threads)
+    ora = O.Oracle(W, H, _options(lib, sc), threads=threads)
     ora.set_volume(vol, sc.medium)
     ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
     ora.render_frame(sc.camera(0))
@@ -145,7 +254,23 @@ def cpu_sample(args, threads, frames=2, scale_w=4, scale_h=4):
     t = float(np.median(times))
     fps = 1.0 / (t * (args.width * args.height) / (W * H))
     per_px = reads.astype(np.float64) / (W * H * len(times))
-    return fps, t, W, H, per_px
+    lp = None
+    if learned is not None:
+        M, params, box = learned
+        scl = _scene(args, fp16=True, width=W, height=H)
+        voll = Volume.procedural(scl.volume, lib=lib)
+        ol = O.Oracle(W, H, _options(lib, scl, True, M), threads=threads)
+        ol.set_volume(voll, scl.medium)
+        ol.set_lights(scl.lights, scl.env_rgb, scl.env_scale)
+        ol.set_net(params, box)
+        ol.render_frame(scl.camera(0))
+        O.voxel_reads()
+        ol.render_frame(scl.camera(1))
+        r = O.voxel_reads().astype(np.float64) / (W * H)
+        q = ol.export_lp(0)
+        lp = {"generate_voxel_reads_px": float(r[0] + r[1]), "select_voxel_reads_px": float(r[7] + r[2]),
+              "vertices_px": float(ol.export_lp(3)[0]) / (W * H), "queries_px": float((q[:, 6] >= 0).sum()) / (W * H)}
+    return fps, t, W, H, per_px, lp
 
 
 def run_reference(args):
@@ -162,8 +287,8 @@ def run_reference(args):
     vbuild.build()
     lib = capi.load()
     threads = os.cpu_count() or 1
-    sc = _scene(args)
     W, H = args.width // 4, args.height // 4
+    sc = _scene(args, width=W, height=H)
     vol = Volume.procedural(sc.volume, lib=lib)
     ora = O.Oracle(W, H, _options(lib, sc), threads=threads)
     ora.set_volume(vol, sc.medium)
@@ -177,9 +302,9 @@ def run_reference(args):
         times.append(time.perf_counter() - t)
     scale = (args.width * args.height) / (W * H)
     fps = args.steps / (sum(times) * scale)
-    sample = (f"oracle (CPU restatement of the reference shaders; the reference itself is D3D12/Slang-only), "
-              f"{args.steps} frames at {W}x{H} after {max(args.warmup, 1)} untimed, scaled by pixel count to "
-              f"{args.width}x{args.height}")
+    sample = (f"oracle (CPU restatement of the reference shaders; the reference itself is D3D12/Slang-only), plain form "
+              f"(FP32 bricks, M=32), {args.steps} frames at {W}x{H} after {max(args.warmup, 1)} untimed, scaled by pixel count "
+              f"to {args.width}x{args.height}")
     line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -216,49 +341,55 @@ def run_gpu(args):
     from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
     vbuild.build()
     lib = capi.load()
-    sc = _scene(args)
-    t0 = time.time()
-    vol = Volume.procedural(sc.volume, lib=lib)
-    build_s = time.time() - t0
-    opts = _options(lib, sc)
     W, H = args.width, args.height
-    rd = VolumetricReSTIR(W, H, opts.as_dict(), lib=lib)
-    rd.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
-    stream = torch.cuda.current_stream()
-    sptr = stream.cuda_stream
-    out = torch.empty((H, W, 4), device="cuda", dtype=torch.float32)
+    t0 = time.time()
+    vols = {False: Volume.procedural(_scene(args).volume, lib=lib), True: Volume.procedural(_scene(args, fp16=True).volume, lib=lib)}
+    build_s = time.time() - t0
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
 
-    # ---- device-resident frames ----
-    for f in range(args.warmup):
-        rd.execute(sc.camera(f), out.data_ptr(), stream=sptr)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    rd.kernel_time_totals(reset=True)
-    launches = 0
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for f in range(args.warmup, args.warmup + args.steps):
-            rd.execute(sc.camera(f), out.data_ptr(), stream=sptr)
-            launches += rd.last_launch_count()
-        e1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    tot, nfr = rd.kernel_time_totals(reset=True)
-    kernel_ms = {"k_initial": tot[0] / max(nfr, 1), "k_spatial": tot[1] / max(nfr, 1)}
-    ms = e0.elapsed_time(e1)
+    # ---- relMSE matching (480x270, static camera, FP64 reference) ----
+    forms = {"plain": (False, False, 32)}
+    for M in LEARNED_M:
+        forms[f"learned_M{M}"] = (True, True, M)
+    rel, qinfo = quality(lib, vols, args, forms) if not args.no_quality else ({}, {})
+    # matched: the learned form's relMSE is not above the plain form's by more than two standard
+    # errors of the difference
+    M_sel, matched = LEARNED_M[0], False
+    if rel:
+        pm, pse = rel["plain"]
+
+        def z(M):
+            lm, lse = rel[f"learned_M{M}"]
+            return (lm - pm) / max(np.hypot(lse, pse), 1e-12)
+        ok = [M for M in LEARNED_M if z(M) <= 2.0]
+        if ok:
+            M_sel, matched = ok[0], True
+        else:
+            M_sel = min(LEARNED_M, key=z)
+
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    out = torch.empty((H, W, 4), device="cuda", dtype=torch.float32)
+    # ---- learned form, device-resident frames ----
+    sc = _scene(args, fp16=True)
+    opts = _options(lib, sc, True, M_sel)
+    rd = VolumetricReSTIR(W, H, opts.as_dict(), lib=lib)
+    rd.setScene(vols[True], sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+    ms, kms, launches, clocks = _time_frames(rd, sc, out, sptr, args.warmup, args.steps, clock_index=local, barrier=barrier)
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * args.steps / (ms / 1000.0)
+    queries = len(rd.export_learned(1)) if rank == 0 else 0
+    net_params, net_box = rd.net_params(), rd.net_box()
+    stage_names = ["initial_stage", "spatial_final", "training", "k_lp_generate", "k_net_infer", "k_lp_select"]
+    kernel_ms = dict(zip(stage_names, kms))
 
-    # ---- end to end through the host entry point ----
+    # ---- learned form, end to end through the host entry point ----
     pinned = torch.empty((H, W, 4), dtype=torch.float32).pin_memory()
     hptr = C.cast(C.c_void_p(pinned.data_ptr()), C.POINTER(C.c_float))
     n0 = args.warmup + args.steps
@@ -274,46 +405,68 @@ def run_gpu(args):
     h2d, d2h = C.c_int64(), C.c_int64()
     lib.vr_last_transfer_bytes(rd._h, C.byref(h2d), C.byref(d2h))
     e2e = ws * args.steps / e2e_s
+    del rd
+
+    # ---- plain form (FP32 bricks, M=32), same frames ----
+    scp = _scene(args)
+    optp = _options(lib, scp)
+    rp = VolumetricReSTIR(W, H, optp.as_dict(), lib=lib)
+    rp.setScene(vols[False], scp.medium, scp.lights, scp.env_rgb, scp.env_scale)
+    msp, kmsp, _, _ = _time_frames(rp, scp, out, sptr, args.warmup, args.steps, barrier=barrier)
+    plain_fps = ws * args.steps / (msp / 1000.0)
+    del rp
 
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel ----
+    # ---- CPU baseline and the per-pixel counts of the roofline ----
     peak, peak_kind = _peaks()
-    fps_cpu, t_cpu, cw, ch, per_px = (None, None, 0, 0, None)
-    cpu = None
+    cpu, lpc = None, None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        fps_cpu, t_cpu, cw, ch, per_px = cpu_sample(args, threads)
+        fps_cpu, t_cpu, cw, ch, per_px, lpc = cpu_sample(args, threads, learned=(M_sel, net_params, net_box))
         cpu = {"value": fps_cpu, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"oracle frame 1 (temporal+spatial) at {cw}x{ch} ({t_cpu:.2f} s), scaled by pixel count to {W}x{H}"}
-    avg = kernel_ms
-    dom = max(avg, key=lambda k: avg[k] or 0.0)
-    roof = None
-    if per_px is not None and avg[dom]:
-        vox_bytes = 2 if sc.volume.fp16 else 4
-        sb = stream_bytes_per_pixel(opts.mMaxBounces, opts.mSpatialSampleCount)
-        vox = {"k_initial": per_px[0] + per_px[1] + per_px[2], "k_spatial": per_px[3] + per_px[4]}
-        alg = (sb[dom] + vox[dom] * vox_bytes) * W * H
-        achieved = alg / (avg[dom] / 1000.0) / 1e9
-        traffic = _traffic_from_profile(dom)
+               "sample": f"oracle, plain form, frame 1 (temporal+spatial) at {cw}x{ch} ({t_cpu:.2f} s), scaled by pixel count to {W}x{H}"}
+    dom = max(("k_lp_generate", "k_net_infer", "k_lp_select", "spatial_final", "training"), key=lambda k: kernel_ms[k] or 0.0)
+    roof, roof_tc = None, None
+    if lpc is not None and kernel_ms["k_lp_generate"]:
+        vox_bytes = 2
+        per_px = lpc["generate_voxel_reads_px"] * vox_bytes + generate_stream_bytes_per_pixel(M_sel, lpc["vertices_px"], lpc["queries_px"])
+        alg = per_px * W * H
+        achieved = alg / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": alg, "voxel_reads_per_pixel": float(vox[dom]),
-                "kernel_ms": avg[dom]}
+                "traffic": _traffic_from_profile("k_lp_generate"), "kernel": "k_lp_generate", "peak_source": peak_kind,
+                "dominant_by_time": dom, "algorithmic_bytes_per_launch": alg, "algorithmic_bytes_per_pixel": per_px,
+                "voxel_reads_per_pixel": lpc["generate_voxel_reads_px"], "vertex_records_per_pixel": lpc["vertices_px"],
+                "queries_per_pixel": lpc["queries_px"], "kernel_ms": kernel_ms["k_lp_generate"],
+                "counts_from": f"oracle, learned form, frame 1 at {args.width // 4}x{args.height // 4}"}
+    if kernel_ms["k_net_infer"]:
+        tf = queries * NET_FLOP_PER_QUERY / (kernel_ms["k_net_infer"] / 1000.0) / 1e12
+        pk = _bf16_peak()
+        roof_tc = {"bound": "tensor", "kernel": "k_net_infer", "achieved": tf, "peak": pk[0], "unit": "TFLOP/s",
+                   "frac": tf / pk[0] if pk[0] else None, "peak_source": pk[1], "queries_per_frame": queries,
+                   "flop_per_query": NET_FLOP_PER_QUERY, "kernel_ms": kernel_ms["k_net_infer"]}
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic",
+            "dtype": "f32 (bf16 MLP, fp16 bricks)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "width": W, "height": H, "max_path_length": opts.mMaxBounces,
-                       "candidates": opts.mInitialM, "spatial_samples": opts.mSpatialSampleCount,
+                       "candidates": M_sel, "spatial_samples": opts.mSpatialSampleCount, "bricks": "fp16",
                        "l2": "inputs larger than L2 (bricks + reservoir buffers), no flush",
                        "parallelism": f"replicas x{ws}", "volume_build_s": round(build_s, 2),
-                       "samples_per_s": value * W * H * (opts.mInitialM + opts.mSpatialSampleCount + 1),
-                       "kernel_ms": avg},
+                       "samples_per_s": value * W * H * (M_sel + opts.mSpatialSampleCount + 1),
+                       "kernel_ms": kernel_ms,
+                       "training": {"samples_per_frame": opts.mLearnedTrainSamples, "batch": opts.mLearnedBatch,
+                                    "lr": opts.mLearnedLearningRate}},
+            "plain": {"value": plain_fps, "unit": "frames/s", "candidates": 32, "bricks": "fp32",
+                      "kernel_ms": {"k_initial": kmsp[0], "k_spatial": kmsp[1]}, "speedup_learned_vs_plain": value / plain_fps},
+            "relmse": {"matched": matched, "criterion": "learned - plain <= 2 standard errors of the difference",
+                       "plain": rel.get("plain"), "learned": rel.get(f"learned_M{M_sel}"),
+                       "all": {k: {"mean": v[0], "se": v[1]} for k, v in rel.items()}, **qinfo},
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": int(h2d.value), "d2h_bytes_per_step": int(d2h.value)},
             "gpu_launches": launches,
             "roofline": roof,
+            "roofline_tensor": roof_tc,
             "cpu_baseline": cpu,
-            "clocks": clk.summary()}
+            "clocks": clocks}
     print(json.dumps(line), flush=True)
 
 
@@ -326,6 +479,7 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-quality", action="store_true", help="skip the relMSE matching (learned form at M=32)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else max(args.warmup, 0)
     if args.impl == "reference":

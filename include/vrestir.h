@@ -118,6 +118,7 @@ typedef struct vr_options {
     float mLearnedTFloor;                       /* 0.02: lower clamp of the predicted transmittance */
     uint32_t mLearnedSeed;                      /* 1: weight initialisation and training streams */
     uint32_t mLearnedTargetMethod;              /* VR_TRACK_RAY_MARCHING: estimator of the training targets (mip 0) */
+    int32_t mLearnedLoss;                       /* 0: squared error of T; 1: squared error of log T (targets floored) */
 } vr_options;
 
 /* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */
@@ -289,9 +290,11 @@ int32_t vr_frame_count(const vr_context* ctx);
 /* ---- instrumentation ---- */
 /* Per-kernel device time of the last vr_render_frame (milliseconds), CUDA events. */
 int vr_last_timings(const vr_context* ctx, float* ms, int32_t max_entries, int32_t* n);
-/* Device time per kernel stage (0: k_initial, 1: spatial/final stage) summed over the frames
- * rendered since the last reset, from CUDA events recorded on the caller's stream.  Waits for
- * those events; call it outside a timed region. */
+/* Device time per kernel stage summed over the frames rendered since the last reset, from CUDA
+ * events recorded on the caller's stream: 0 initial stage (k_initial, or generate + infer +
+ * select with the learned target), 1 spatial/final stage, 2 network training, 3 generate,
+ * 4 infer, 5 select (up to 8 entries).  Waits for those events; call it outside a timed
+ * region. */
 int vr_kernel_time_totals(vr_context* ctx, float* ms, int32_t max_entries, int32_t* frames, int32_t reset);
 /* Kernel launches issued by the last vr_render_frame. */
 int32_t vr_last_launch_count(const vr_context* ctx);

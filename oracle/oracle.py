@@ -42,7 +42,7 @@ def _load():
         "vro_set_lp_T": (None, [P, P, C.c_int64]),
         "vro_export_lp": (C.c_int64, [P, C.c_int, P, C.c_int64]),
         "vro_net_forward": (None, [P, P, P, C.c_float, P, C.c_int, P]),
-        "vro_net_gradients": (None, [P, P, P, P, C.c_int, P, P]),
+        "vro_net_gradients": (None, [P, P, P, P, C.c_int, C.c_int, C.c_float, P, P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -170,7 +170,8 @@ class Oracle:
 
 
 def voxel_reads():
-    """Voxel reads per pass since the last call: features, initial, temporal, spatial, final, reference."""
+    """Voxel reads per pass since the last call: features, initial, temporal, spatial, final,
+    reference, (unused), and the learned-target select share (p_hat of the winner)."""
     out = np.zeros(8, np.uint64)
     lib().vro_voxel_reads(_ptr(out))
     return out
@@ -201,12 +202,12 @@ def net_forward(params, box, floor, queries):
     return out
 
 
-def net_gradients(params, box, samples):
-    """Loss and gradient of the training step, summed in the training kernel's order."""
+def net_gradients(params, box, samples, loss_log=0, floor=0.02):
+    """Loss and gradient of the training step with the training kernel's numerics."""
     s = np.ascontiguousarray(samples, np.float32).reshape(-1, 8)
     P = np.ascontiguousarray(params, np.float32)
     b0, b1 = [np.ascontiguousarray(b, np.float32) for b in box]
     g = np.zeros(len(P), np.float32)
     loss = np.zeros(1, np.float32)
-    lib().vro_net_gradients(_ptr(P), _ptr(b0), _ptr(b1), _ptr(s), len(s), _ptr(g), _ptr(loss))
+    lib().vro_net_gradients(_ptr(P), _ptr(b0), _ptr(b1), _ptr(s), len(s), int(loss_log), float(floor), _ptr(g), _ptr(loss))
     return float(loss[0]), g

@@ -235,7 +235,10 @@ static f3 nodeVmin(const Slot& s, int lev, int id) {
 }
 
 // instrumentation: voxel reads per pass (algorithmic brick bytes for the roofline)
+// voxel reads per pass (instrumentation for the roofline's algorithmic bytes); a pass may
+// attribute part of its reads to another counter through tl_voxSplit
 static thread_local uint64_t tl_voxReads = 0;
+static thread_local uint64_t tl_voxSplit = 0;
 static std::atomic<uint64_t> g_voxReads[8];
 static float voxel(const Slot& s, int brick, int x, int y, int z) {     // local coords in [-1, 8]
     ++tl_voxReads;
@@ -1256,7 +1259,8 @@ static float predict(float o, float floor_) {
 // gradient of mean((exp(o) - target)^2) with the training kernel's numerics: BF16 weights,
 // activations and dZ, FP32 sums (per chunk of 128 samples in sample order, then chunk sums in
 // chunk order; the tensor core's own order inside the products differs)
-static void gradients(const float* P, const float* samples, int n, const float bmin[3], const float binv[3], float* grad, float* loss) {
+static void gradients(const float* P, const float* samples, int n, const float bmin[3], const float binv[3], int lossLog, float floor_,
+                      float* grad, float* loss) {
     const float invB = 1.f / (float)n;
     std::vector<float> tot(kParams, 0.f), part(kParams);
     float lossTot = 0.f;
@@ -1291,10 +1295,17 @@ static void gradients(const float* P, const float* samples, int n, const float b
             }
             (void)o;
             if (valid) {
-                float p = exp_(o);
-                float d = p - samples[(size_t)si * 8 + 7];
-                g[t] = 2.f * d * p * invB;
-                lv[t] = d * d * invB;
+                const float y = samples[(size_t)si * 8 + 7];
+                if (lossLog) {
+                    float d = o - log_(fmax_(y, floor_));
+                    g[t] = 2.f * d * invB;
+                    lv[t] = d * d * invB;
+                } else {
+                    float p = exp_(o);
+                    float d = p - y;
+                    g[t] = 2.f * d * p * invB;
+                    lv[t] = d * d * invB;
+                }
             }
             for (int k = 0; k < kHid; ++k) dhs[(size_t)t * 64 + k] = g[t] * rb(P[kOutW + k]);
         }
@@ -1678,6 +1689,7 @@ struct Oracle {
     float lpBmin[3] = {0, 0, 0}, lpBinv[3] = {1, 1, 1};
     std::vector<float> lpTIn;
     std::vector<float> lpQueries, lpTrain, lpTUsed;
+    std::atomic<int64_t> lpVertices{0};     // vertex records written by the last learned-target frame
 
     int curPass = 0;     // 0 features, 1 initial, 2 temporal, 3 spatial, 4 final, 5 reference
     template <class F>
@@ -1686,8 +1698,10 @@ struct Oracle {
         const int pass = curPass;
         auto row = [&](int y) {
             tl_voxReads = 0;
+            tl_voxSplit = 0;
             f(y);
-            g_voxReads[pass] += tl_voxReads;
+            g_voxReads[pass] += tl_voxReads - tl_voxSplit;
+            g_voxReads[7] += tl_voxSplit;
         };
         if (nt <= 1) { for (int y = 0; y < H; ++y) row(y); return; }
         std::atomic<int> next(0);
@@ -1807,6 +1821,7 @@ struct Oracle {
         lpTUsed.assign((size_t)M * mb * N, 0.f);
         const bool haveT = lpTIn.size() == (size_t)M * mb * N;
         std::atomic<bool> ll(false);
+        lpVertices = 0;
         forRows([&](int y) {
             Ctx cl = c;
             std::vector<LpVertex> rec((size_t)M * mb);
@@ -1826,6 +1841,9 @@ struct Oracle {
                                                              &ex[(size_t)cid * std::max(mb - 1, 1)], q.data());
                         crec[cid * 2] = depth;
                         crec[cid * 2 + 1] = next1D(sg);
+                        int nv = 0;
+                        for (int b = 0; b < mb; ++b) nv += (rec[(size_t)cid * mb + b].flags & kLpValid) ? 1 : 0;
+                        lpVertices += nv;
                         for (int b = 0; b < mb; ++b) {
                             const size_t slot = (size_t)(cid * mb + b) * N + pid;
                             if (rec[(size_t)cid * mb + b].flags & kLpNeedsT) {
@@ -1872,7 +1890,9 @@ struct Oracle {
                     }
                 }
                 ExtraProvider prov{finalExtra};
+                const uint64_t r0 = tl_voxReads;
                 float p_hat = evaluate_P_hat(cl, ray, sg, prov, c.spatial, fin);
+                tl_voxSplit += tl_voxReads - r0;      // the select kernel's share
                 if (fin.runningSum > 0.f) {
                     fin.runningSum *= fin.p_y == 0.f ? 0.f : p_hat / fin.p_y;
                     fin.p_y = p_hat;
@@ -2540,9 +2560,14 @@ void vro_set_lp_T(void* h, const float* T, int64_t n) {
     if (!T || n <= 0) p->lpTIn.clear();
     else p->lpTIn.assign(T, T + n);
 }
-// which 0: per-slot queries (8 floats, tmax = -1 where none), 1: T used per slot, 2: training samples
+// which 0: per-slot queries (8 floats, tmax = -1 where none), 1: T used per slot, 2: training samples,
+// 3: vertex records written by the last frame (one value)
 int64_t vro_export_lp(void* h, int which, float* out, int64_t cap) {
     Oracle* p = (Oracle*)h;
+    if (which == 3) {
+        if (out && cap >= 1) out[0] = (float)p->lpVertices.load();
+        return 1;
+    }
     const std::vector<float>& v = which == 0 ? p->lpQueries : which == 1 ? p->lpTUsed : p->lpTrain;
     if (out && cap >= (int64_t)v.size()) memcpy(out, v.data(), v.size() * sizeof(float));
     return (int64_t)v.size();
@@ -2554,8 +2579,9 @@ void vro_net_forward(const float* params, const float bmin[3], const float binv[
         out[i] = oracle::lpo::predict(o, floor_);
     }
 }
-void vro_net_gradients(const float* params, const float bmin[3], const float binv[3], const float* samples, int n, float* grads, float* loss) {
-    oracle::lpo::gradients(params, samples, n, bmin, binv, grads, loss);
+void vro_net_gradients(const float* params, const float bmin[3], const float binv[3], const float* samples, int n, int lossLog, float floor_,
+                       float* grads, float* loss) {
+    oracle::lpo::gradients(params, samples, n, bmin, binv, lossLog, floor_, grads, loss);
 }
 
 }  // extern "C"

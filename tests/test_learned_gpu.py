@@ -71,16 +71,17 @@ def _same(a, b):
     return np.array_equal(np.asarray(a, np.float32).view(np.uint32), np.asarray(b, np.float32).view(np.uint32))
 
 
-def test_net_gradients_match_oracle(vlib, cuda):
+@pytest.mark.parametrize("loss_log", [0, 1])
+def test_net_gradients_match_oracle(vlib, cuda, loss_log):
     from oracle.oracle import net_gradients
-    sc, vol, opts, gpu, ora = _ctx(vlib, cuda)
+    sc, vol, opts, gpu, ora = _ctx(vlib, cuda, dict(mLearnedLoss=loss_log))
     box = gpu.net_box()
     p = _params(3)
     gpu.set_net_params(p)
     s = _samples(4, 1000, box)                       # 8 CTAs, the last one partial
     d = cuda.from_numpy(s).cuda()
     loss, g = gpu.net_gradients(d.data_ptr(), len(s))
-    lo, go = net_gradients(p, box, s)
+    lo, go = net_gradients(p, box, s, loss_log, opts.mLearnedTFloor)
     assert np.isfinite(loss) and loss > 0
     assert abs(loss - lo) <= 1e-3 * lo, (loss, lo)
     for name, sl in (("hidden 0", slice(0, 4160)), ("hidden 1", slice(4160, 8320)), ("hidden 2", slice(8320, 12480)),
@@ -111,8 +112,8 @@ def test_net_adam_step_bit_exact(vlib, cuda):
     want = p - lr * (m / c1) / (np.sqrt(v / c2) + f(1e-8))
     assert _same(p1, want.astype(np.float32))
     # the step moved the weights and lowered the loss on its batch
-    loss0, _ = net_gradients(p, box, s)
-    loss1, _ = net_gradients(p1, box, s)
+    loss0, _ = net_gradients(p, box, s, 0, opts.mLearnedTFloor)
+    loss1, _ = net_gradients(p1, box, s, 0, opts.mLearnedTFloor)
     assert loss1 < loss0
 
 

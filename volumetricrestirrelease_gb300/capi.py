@@ -43,7 +43,7 @@ class Options(C.Structure):
         ("mFinalLightTrackingMethod", _u32), ("mFinalTStepScale", _f32),
         ("mUseLearnedPHat", _i32), ("mLearnedTrainSamples", _i32), ("mLearnedBatch", _i32),
         ("mLearnedLearningRate", _f32), ("mLearnedTFloor", _f32), ("mLearnedSeed", _u32),
-        ("mLearnedTargetMethod", _u32),
+        ("mLearnedTargetMethod", _u32), ("mLearnedLoss", _i32),
     ]
 
     def as_dict(self):

@@ -235,7 +235,7 @@ struct vr_context {
     int nev = 0;
     std::vector<std::vector<cudaEvent_t>> pendingEv;
     std::vector<cudaEvent_t> freeEv;
-    double totalMs[4] = {0, 0, 0, 0};
+    double totalMs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int totalFrames = 0;
     int launches = 0;
     int64_t h2d = 0, d2h = 0;
@@ -379,6 +379,7 @@ static vrd::NetView net_view(const vr_context* c) {
     v.wbf = c->netWbf; v.bias = c->netBias;
     for (int i = 0; i < 3; ++i) { v.bmin[i] = c->netBmin[i]; v.binv[i] = c->netBinv[i]; }
     v.floor_ = c->opts.mLearnedTFloor;
+    v.lossLog = c->opts.mLearnedLoss;
     return v;
 }
 
@@ -452,6 +453,7 @@ static bool options_valid(const vr_options* o, std::string& why) {
         if (!(o->mLearnedLearningRate >= 0.f) || !(o->mLearnedLearningRate < 1.f)) { why = "mLearnedLearningRate must be in [0, 1)"; return false; }
         if (!(o->mLearnedTFloor > 0.f) || !(o->mLearnedTFloor <= 1.f)) { why = "mLearnedTFloor must be in (0, 1]"; return false; }
         if (o->mLearnedTargetMethod > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown mLearnedTargetMethod"; return false; }
+        if (o->mLearnedLoss < 0 || o->mLearnedLoss > 1) { why = "mLearnedLoss must be 0 or 1"; return false; }
     }
     return true;
 }
@@ -543,6 +545,7 @@ void vr_options_default(vr_options* o) {
     o->mLearnedTFloor = 0.02f;
     o->mLearnedSeed = 1;
     o->mLearnedTargetMethod = VR_TRACK_RAY_MARCHING;
+    o->mLearnedLoss = 0;
 }
 
 // ---- volumes ----
@@ -1001,18 +1004,21 @@ int vr_last_timings(const vr_context* c, float* ms, int32_t max_entries, int32_t
 }
 int32_t vr_last_launch_count(const vr_context* c) { return c ? c->launches : 0; }
 
-// frame events: start, after the initial stage, after the spatial/final stage, after the
-// network training (learned target only); totals: 0 initial, 1 spatial/final, 2 training
+// frame events, plain: start, after the initial stage, after the spatial/final stage, end;
+// learned target: start, after generate, after infer, after select, after the spatial/final
+// stage, after the training.  Totals: 0 initial stage, 1 spatial/final stage, 2 training,
+// 3 generate, 4 infer, 5 select
 static void drain_events(vr_context* c) {
     for (auto& v : c->pendingEv) {
         cudaEventSynchronize(v.back());
-        if (v.size() == 4) {
-            const int map[3][3] = {{0, 1, 0}, {1, 2, 1}, {2, 3, 2}};
-            for (auto& m : map) {
-                float t = 0.f;
-                cudaEventElapsedTime(&t, v[m[0]], v[m[1]]);
-                c->totalMs[m[2]] += t;
-            }
+        static const int plain[3][3] = {{0, 1, 0}, {1, 2, 1}, {2, 3, 2}};
+        static const int learned[6][3] = {{0, 3, 0}, {3, 4, 1}, {4, 5, 2}, {0, 1, 3}, {1, 2, 4}, {2, 3, 5}};
+        const int (*map)[3] = v.size() == 6 ? learned : plain;
+        const int nm = v.size() == 6 ? 6 : (v.size() == 4 ? 3 : 0);
+        for (int i = 0; i < nm; ++i) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, v[map[i][0]], v[map[i][1]]);
+            c->totalMs[map[i][2]] += t;
         }
         c->totalFrames++;
         for (auto e : v) c->freeEv.push_back(e);
@@ -1022,7 +1028,7 @@ static void drain_events(vr_context* c) {
 int vr_kernel_time_totals(vr_context* c, float* ms, int32_t max_entries, int32_t* frames, int32_t reset) {
     if (!c || !ms || !frames) return VR_ERR_INVALID_ARG;
     drain_events(c);
-    for (int i = 0; i < max_entries && i < 4; ++i) ms[i] = (float)c->totalMs[i];
+    for (int i = 0; i < max_entries && i < 8; ++i) ms[i] = (float)c->totalMs[i];
     *frames = c->totalFrames;
     if (reset) { for (double& t : c->totalMs) t = 0; c->totalFrames = 0; }
     return VR_OK;
@@ -1214,12 +1220,21 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         cudaEventRecord(e, st);
         frameEv.push_back(e);
     };
+    auto rec = [&]() {
+        cudaEvent_t e;
+        if (!c->freeEv.empty()) { e = c->freeEv.back(); c->freeEv.pop_back(); }
+        else cudaEventCreate(&e);
+        cudaEventRecord(e, st);
+        frameEv.push_back(e);
+    };
     mark();
     const bool lpOn = lp_active(c);
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
+        rec();
         vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
+        rec();
         launch_lp_select<MB>(P, B, c->lp, grid, block, st);
         c->launches += 3;
         c->lpFrameDone = true;
@@ -1276,11 +1291,7 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         }
         mark();
     } else {
-        cudaEvent_t e;
-        if (!c->freeEv.empty()) { e = c->freeEv.back(); c->freeEv.pop_back(); }
-        else cudaEventCreate(&e);
-        cudaEventRecord(e, st);
-        frameEv.push_back(e);
+        rec();
     }
     c->pendingEv.push_back(frameEv);
     if (c->pendingEv.size() > 512) drain_events(c);

@@ -223,7 +223,8 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
 // dW_l = dZ_l^T X_l (128x64, K = 128 samples); both products accumulate in FP32 in TMEM.  The
 // output layer and the biases are reduced on the CUDA cores.  The CTA writes its gradient to
 // its own row of `partials` (no atomics: a step is deterministic).
-// Loss: mean over the batch of (T - target)^2 with T = exp(o); samples with tmax < 0 add zero.
+// Loss: mean over the batch of (T - target)^2 with T = exp(o), or of (o - log max(target, floor))^2;
+// samples with tmax < 0 add zero.
 namespace ts {
 constexpr int W = 0;               // 4 x 8192: W_l, [64 out][64 in] K-major (forward B operand)
 constexpr int WT = 32768;          // 3 x 8192: W_l^T for l = 1..3, [64 in][64 out] K-major (dH B operand)
@@ -348,10 +349,17 @@ __global__ void __launch_bounds__(128, 1) k_net_train(NetView net, const float4*
         o += *sB4;
         float lv = 0.f;
         if (valid) {
-            const float p = vr::exp_(o);
-            const float d = p - samples[2 * (size_t)si + 1].w;
-            g = 2.f * d * p * invB;
-            lv = d * d * invB;
+            const float y = samples[2 * (size_t)si + 1].w;
+            if (net.lossLog) {
+                const float d = o - vr::log_(vr::fmax_(y, net.floor_));
+                g = 2.f * d * invB;
+                lv = d * d * invB;
+            } else {
+                const float p = vr::exp_(o);
+                const float d = p - y;
+                g = 2.f * d * p * invB;
+                lv = d * d * invB;
+            }
         }
         sG[tid] = g;
         sL[tid] = lv;

@@ -23,6 +23,7 @@ struct NetView {
     const float* bias;     // FP32 biases: 4 x 64 hidden, then the output bias
     float bmin[3], binv[3];
     float floor_;          // lower clamp of the predicted transmittance
+    int lossLog;           // training loss: 0 squared error of T, 1 squared error of log T
 };
 
 // vertex record flags

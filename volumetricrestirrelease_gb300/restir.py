@@ -181,10 +181,10 @@ class VolumetricReSTIR:
         return list(ms[: n.value])
 
     def kernel_time_totals(self, reset=True):
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * 8)()
         n = C.c_int32()
-        self._check(self._lib.vr_kernel_time_totals(self._h, ms, 4, C.byref(n), 1 if reset else 0))
-        return list(ms[:3]), n.value
+        self._check(self._lib.vr_kernel_time_totals(self._h, ms, 8, C.byref(n), 1 if reset else 0))
+        return list(ms[:6]), n.value
 
     def last_launch_count(self):
         return self._lib.vr_last_launch_count(self._h)
