@@ -226,6 +226,18 @@ void vr_volume_destroy(vr_volume* v);
 int vr_volume_get_info(const vr_volume* v, vr_volume_info* info);
 int vr_volume_get_slot(const vr_volume* v, int32_t slot, vr_grid_view* view);
 
+/* Fire plume (synthetic stand-in for the reference's emissive .vbx sequences): a density volume
+ * (column widening with height, fBm turbulence, density falling off with height) and a
+ * temperature volume (mip 0 only) over the same box, t_min..t_max kelvin inside the plume and
+ * 0 outside.  d->kind, mask_radius and threshold are ignored. */
+int vr_volume_create_fire(const vr_procedural_desc* d, float t_min, float t_max, vr_volume** density,
+                          vr_volume** temperature);
+/* Blackbody colours of 50 K .. 6400 K in 50 K steps (128 RGB triples, linear sRGB): Planck's law
+ * integrated against the CIE 1931 colour-matching functions (multi-lobe Gaussian fit of Wyman,
+ * Sloan and Shirley, 2013), normalised to unit luminance at 6400 K.  The project's own table in
+ * the role of the reference's LUT/BlackBodyRadiationRGB_50K-6400K.txt (Scene.cpp:2877-2893). */
+void vr_blackbody_lut(float rgb[384]);
+
 /* ---- context lifecycle (getPasses/create, VolumetricReSTIR.cpp:61-70) ---- */
 vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int32_t* err);
 void vr_destroy(vr_context* ctx);
@@ -239,6 +251,14 @@ int vr_resize(vr_context* ctx, int32_t width, int32_t height);
 int vr_set_volume(vr_context* ctx, const vr_volume* vol, const vr_medium* medium);
 int vr_set_lights(vr_context* ctx, const vr_point_light* lights, int32_t num_lights,
                   const vr_env_map* env);
+/* Volume emission (hasEmissionGrid, LeScale, temperatureCutOff, temperatureScale of
+ * Scene::addGVDBVolume, Scene.cpp:2754; Emission / ConvertTempToColor, VolumeBase.slang:
+ * 196-232): Le(x) = le_scale * LUT((min(6400, (T(x) - cutoff) * scale) - 25) / 6400), T the
+ * trilinear temperature at mip 0, the 128-texel table read with linear filtering between texel
+ * centres and clamped at its ends.  lut_rgb: 128 RGB triples or NULL for vr_blackbody_lut's.
+ * temperature NULL switches emission off.  Resets the history like an option change. */
+int vr_set_emission(vr_context* ctx, const vr_volume* temperature, float le_scale, float cutoff,
+                    float scale, const float* lut_rgb);
 
 /* ---- per-frame call (execute, VolumetricReSTIR.cpp:303-906) ----
  * out_rgba_device: width*height float4 (RGBA32F, `accumulated_color`), device memory.

@@ -39,6 +39,7 @@ def _load():
         "vro_xoshiro": (None, [P, C.c_int, P]),
         "vro_splitmix": (None, [C.c_uint64, C.c_int, P]),
         "vro_set_net": (None, [P, P, P, P]),
+        "vro_set_emission": (None, [P, P, P, C.c_float, C.c_float, C.c_float]),
         "vro_set_lp_T": (None, [P, P, C.c_int64]),
         "vro_export_lp": (C.c_int64, [P, C.c_int, P, C.c_int64]),
         "vro_net_forward": (None, [P, P, P, C.c_float, P, C.c_int, P]),
@@ -114,6 +115,16 @@ class Oracle:
         if r != 0:
             raise RuntimeError(f"oracle reference status {r}")
         return accum
+
+    def set_emission(self, temperature, le_scale, cutoff=0.0, scale=1.0, lut=None):
+        from volumetricrestirrelease_gb300.restir import blackbody_lut
+        if temperature is None:
+            self.L.vro_set_emission(self._h, None, None, 0.0, 0.0, 1.0)
+            return
+        self._tview = temperature.slot(0)
+        self._tvol = temperature
+        self._lut = np.ascontiguousarray(blackbody_lut() if lut is None else lut, np.float32).reshape(384)
+        self.L.vro_set_emission(self._h, C.byref(self._tview), _ptr(self._lut), le_scale, cutoff, scale)
 
     # ---- learned target ----
     def set_net(self, params, box):

@@ -175,12 +175,20 @@ struct MediumI {
     int numMips;
 };
 
+struct Emission {             // VolumeDesc.hasEmission, LeScale, temperatureCutOff/Scale + the LUT
+    bool has = false;
+    Slot slot;                 // temperature grid, mip 0
+    float leScale = 0.f, cutoff = 0.f, scale = 1.f;
+    float lut[128][3];
+};
+
 struct Scene {
     Slot slots[VR_NUM_SLOTS];
     MediumI med;
     std::vector<vr_point_light> lights;
     EnvMap env;
     bool hasEnv = false;
+    Emission emis;
 };
 
 // ---------------------------------------------------------------------------------------
@@ -303,6 +311,36 @@ static float Density(const Scene& sc, f3 p, int mip) {
     return trilinear(s, br, p - vmin) * sc.med.dscale;
 }
 static float DensityWorldSpace(const Scene& sc, f3 p, int mip) { return Density(sc, WorldToMediumP(sc, p, mip), mip); }
+
+// TemperatureWorldSpace / ConvertTempToColor / EmissionWorldSpace (VolumeBase.slang:196-232);
+// the LUT's hardware linear filter restated in software: texel centres at (i + 0.5) / 128,
+// clamped addressing
+static float TemperatureWorldSpace(const Scene& sc, f3 pw) {
+    const Slot& s = sc.emis.slot;
+    f3 p = mulPoint(pw, s.M);
+    if (p.x < s.bmin[0] || p.y < s.bmin[1] || p.z < s.bmin[2] || p.x >= s.bmax[0] || p.y >= s.bmax[1] || p.z >= s.bmax[2]) return 0.f;
+    f3 vmin;
+    int br = findBrick(s, p, vmin);
+    if (br < 0) return 0.f;
+    return trilinear(s, br, p - vmin);
+}
+static f3 ConvertTempToColor(const Scene& sc, float temp) {
+    temp = fmin_(6400.f, (temp - sc.emis.cutoff) * sc.emis.scale);
+    const float q = (temp - 25.f) / 6400.f;
+    const float x = q * 128.f - 0.5f;
+    const float fl = floor_(x);
+    const float f = x - fl;
+    int i0 = f2i(fl), i1 = i0 + 1;
+    i0 = std::min(127, std::max(0, i0));
+    i1 = std::min(127, std::max(0, i1));
+    const f3 a = mk3(sc.emis.lut[i0][0], sc.emis.lut[i0][1], sc.emis.lut[i0][2]);
+    const f3 b = mk3(sc.emis.lut[i1][0], sc.emis.lut[i1][1], sc.emis.lut[i1][2]);
+    return sc.emis.leScale * (a + (b - a) * f);
+}
+static f3 EmissionWorldSpace(const Scene& sc, f3 pw) {
+    if (!sc.emis.has) return mk3(0.f);
+    return ConvertTempToColor(sc, TemperatureWorldSpace(sc, pw));
+}
 
 // Bounds3f::IntersectP + IntersectVolumeBound (VolumeBase.slang:131-172)
 static bool IntersectVolumeBound(const Scene& sc, const Ray& ray, float& tMin, float& tMax, int mip, bool vertexCenter) {
@@ -1132,6 +1170,7 @@ static Reservoir ComputeInitialSample(Ctx& c, Ray primaryRay, float preHit, floa
                 out.lightID = -1; out.lightUV[0] = 0; out.lightUV[1] = 0;
                 float outLightPdf = 0.f, outVisibility = 1.f;
                 f3 Ld = mk3(0.f), Le = mk3(0.f);
+                if (sc.emis.has && actualVolumeDensity > 0.f) Le = EmissionWorldSpace(sc, mi.p);
                 f3 one_minus_albedo = mk3(1.f) - albedo;
                 bool shouldComputeLightVisibility = options.lightSamples == 0 ? false : true;
                 Ld = SampleDirectLighting(c, sg, outLightPdf, mi, options, shouldComputeLightVisibility, out.lightID, out.lightUV, outVisibility);
@@ -1411,6 +1450,7 @@ static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf,
                 out.lightID = -1; out.lightUV[0] = 0; out.lightUV[1] = 0;
                 float outLightPdf = 0.f;
                 f3 Ld = mk3(0.f), Le = mk3(0.f);
+                if (sc.emis.has && actualVolumeDensity > 0.f) Le = EmissionWorldSpace(sc, mi.p);
                 f3 one_minus_albedo = mk3(1.f) - albedo;
                 SceneLightSample ls;
                 bool lv = sampleSceneLights(sc, mi.p, options.useEnvironmentLights, options.useAnalyticLights, sg, ls, out.lightID, out.lightUV);
@@ -1543,7 +1583,7 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
         if (isBackgroundSample) {
             F = F * envEval(sc, ray.dir);
         } else if (isSelfEmission) {
-            F = F * mk3(0.f);              // EmissionWorldSpace: no emission grid on this path
+            F = F * EmissionWorldSpace(*c.sc, p_World);
         } else {
             bool isScatterSelfEmission = false;
             Ray scatterRay{};
@@ -1592,7 +1632,7 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                     mi.p = p_World;
                     if (all_eq0(F)) return mk3(0.f);
                 }
-                if (isScatterSelfEmission) F = F * mk3(0.f);
+                if (isScatterSelfEmission) F = F * EmissionWorldSpace(*c.sc, p_World);
                 else mi = MediumInteraction{scatterRay.at(scatterRay.tMax), -scatterRay.dir, sc.med.g, true};
             }
             if (!isScatterSelfEmission && any_gt0(F))
@@ -1977,7 +2017,7 @@ struct Oracle {
             if (mi.isValid) {
                 f3 albedo = s.med.sigma_s / s.med.sigma_t;
                 f3 one_minus_albedo = mk3(1.f) - albedo;
-                { f3 Le = mk3(0.f); L = L + Le * one_minus_albedo * beta; }
+                { f3 Le = EmissionWorldSpace(s, mi.p); L = L + Le * one_minus_albedo * beta; }
                 beta = beta * albedo;
                 if (useNEE) {
                     // directLighting (VolumeUtils.slang:453-483)
@@ -2362,14 +2402,8 @@ void vro_set_options(void* h, const vr_options* o) {
     p->optionsChanged = true;
 }
 
-int vro_set_volume(void* h, const vr_grid_view* views, int numViews, const vr_medium* m, float voxelSize, float superDiag, int numMips) {
-    Oracle* p = (Oracle*)h;
-    oracle::Scene& sc = p->sc;
-    for (int s = 0; s < VR_NUM_SLOTS; ++s) sc.slots[s] = oracle::Slot();
-    for (int s = 0; s < numViews && s < VR_NUM_SLOTS; ++s) {
-        const vr_grid_view& v = views[s];
-        oracle::Slot& d = sc.slots[s];
-        if (!v.valid) continue;
+static void load_slot(const vr_grid_view& v, oracle::Slot& d) {
+    {
         d.valid = true;
         for (int i = 0; i < 3; ++i) { d.res[i] = v.res[i]; d.bmin[i] = v.bmin[i]; d.bmax[i] = v.bmax[i]; }
         memcpy(d.M, v.world_to_index, sizeof(d.M));
@@ -2393,6 +2427,14 @@ int vro_set_volume(void* h, const vr_grid_view* views, int numViews, const vr_me
             }
         }
     }
+}
+
+int vro_set_volume(void* h, const vr_grid_view* views, int numViews, const vr_medium* m, float voxelSize, float superDiag, int numMips) {
+    Oracle* p = (Oracle*)h;
+    oracle::Scene& sc = p->sc;
+    for (int s = 0; s < VR_NUM_SLOTS; ++s) sc.slots[s] = oracle::Slot();
+    for (int s = 0; s < numViews && s < VR_NUM_SLOTS; ++s)
+        if (views[s].valid) load_slot(views[s], sc.slots[s]);
     sc.med.sigma_s = mk3(m->sigma_s[0], m->sigma_s[1], m->sigma_s[2]);
     sc.med.sigma_a = mk3(m->sigma_a[0], m->sigma_a[1], m->sigma_a[2]);
     sc.med.sigma_t = m->sigma_s[0] + m->sigma_a[0];
@@ -2547,6 +2589,19 @@ void vro_xoshiro(const uint32_t seed[4], int draws, uint32_t* out) {
 void vro_splitmix(uint64_t seed, int draws, uint64_t* out) {
     uint64_t st = seed;
     for (int j = 0; j < draws; ++j) out[j] = splitmix64_next(st);
+}
+
+// volume emission: temperature view (mip 0), 128 RGB table, LeScale, cutoff, scale; view NULL = off
+void vro_set_emission(void* h, const vr_grid_view* tview, const float* lut, float leScale, float cutoff, float scale) {
+    Oracle* p = (Oracle*)h;
+    oracle::Emission& e = p->sc.emis;
+    e = oracle::Emission();
+    p->optionsChanged = true;
+    if (!tview || !tview->valid) return;
+    load_slot(*tview, e.slot);
+    memcpy(e.lut, lut, sizeof(e.lut));
+    e.leScale = leScale; e.cutoff = cutoff; e.scale = scale;
+    e.has = true;
 }
 
 // learned target (test infrastructure)

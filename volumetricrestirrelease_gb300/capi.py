@@ -97,6 +97,9 @@ _P = C.c_void_p
 SIGNATURES = {
     "vr_options_default": (None, [C.POINTER(Options)]),
     "vr_volume_create_procedural": (_i32, [C.POINTER(ProceduralDesc), C.POINTER(_P)]),
+    "vr_volume_create_fire": (_i32, [C.POINTER(ProceduralDesc), _f32, _f32, C.POINTER(_P), C.POINTER(_P)]),
+    "vr_blackbody_lut": (None, [C.POINTER(_f32)]),
+    "vr_set_emission": (_i32, [_P, _P, _f32, _f32, _f32, C.POINTER(_f32)]),
     "vr_volume_create_dense": (_i32, [C.POINTER(_f32), _i32, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
     "vr_volume_destroy": (None, [_P]),
     "vr_volume_get_info": (_i32, [_P, C.POINTER(VolumeInfo)]),

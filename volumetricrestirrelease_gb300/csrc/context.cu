@@ -216,6 +216,7 @@ struct vr_context {
     bool hasVolume = false;
     int numMips = 0;
     std::vector<void*> envAllocs;
+    std::vector<void*> emisAllocs;
     HostEnv env;
     // buffers
     vrd::ResBuf res[3]{};      // 0 = perPixel[0], 1 = perPixel[1], 2 = temporal history
@@ -634,6 +635,7 @@ void vr_destroy(vr_context* c) {
     free_net(c);
     for (void* p : c->sceneAllocs) cudaFree(p);
     for (void* p : c->envAllocs) cudaFree(p);
+    for (void* p : c->emisAllocs) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     for (auto& v : c->pendingEv) for (auto e : v) cudaEventDestroy(e);
     for (auto e : c->freeEv) cudaEventDestroy(e);
@@ -664,6 +666,75 @@ int vr_resize(vr_context* c, int32_t w, int32_t h) {
 }
 
 // ---- scene binding ----
+int vr_volume_create_fire(const vr_procedural_desc* d, float t_min, float t_max, vr_volume** density, vr_volume** temperature) {
+    if (!d || !density || !temperature) return VR_ERR_INVALID_ARG;
+    if (d->res <= 0 || d->res > 4096 || d->num_mips < 1 || d->num_mips > VR_NUM_MAX_MIPS || d->octaves < 1 || d->octaves > 16) return VR_ERR_INVALID_ARG;
+    if (d->res % (8 << (d->num_mips - 1)) != 0 || !(d->voxel_size > 0.f) || !(t_min >= 0.f) || !(t_max >= t_min)) return VR_ERR_INVALID_ARG;
+    try {
+        std::vector<float> g, t;
+        vr::procedural_fire(*d, t_min, t_max, g, t);
+        vr_volume* v = new vr_volume();
+        vr_volume* w = new vr_volume();
+        if (vr::build_volume(g, d->res, d->num_mips, d->world_min, d->voxel_size, d->fp16 != 0, v->v) != 0 ||
+            vr::build_volume(t, d->res, 1, d->world_min, d->voxel_size, d->fp16 != 0, w->v) != 0) {
+            delete v; delete w;
+            return VR_ERR_INVALID_ARG;
+        }
+        *density = v;
+        *temperature = w;
+        return VR_OK;
+    } catch (...) {
+        return VR_ERR_OOM;
+    }
+}
+
+void vr_blackbody_lut(float rgb[384]) {
+    if (rgb) vr::blackbody_lut(rgb);
+}
+
+int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float cutoff, float scale, const float* lut) {
+    if (!c) return VR_ERR_INVALID_ARG;
+    for (void* p : c->emisAllocs) cudaFree(p);
+    c->emisAllocs.clear();
+    memset(&c->scene.tslot, 0, sizeof(c->scene.tslot));
+    c->scene.hasEmission = 0;
+    c->optionsChanged = true;
+    if (!temp) return VR_OK;
+    if (!(le_scale >= 0.f) || vr::isinf_(le_scale) || !(scale == scale) || !(cutoff == cutoff)) { c->err = "invalid emission parameters"; return VR_ERR_INVALID_ARG; }
+    const vr::GridSlot& g = temp->v.slots[0];
+    if (!g.valid) { c->err = "temperature volume has no mip 0"; return VR_ERR_INVALID_ARG; }
+    auto up = [&](const void* src, size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        c->emisAllocs.push_back(p);
+        if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+        return p;
+    };
+    vrd::DevSlot& d = c->scene.tslot;
+    d.valid = 1;
+    d.res = g.res;
+    d.bmaxf = (float)g.res;
+    d.maxValue = g.max_value;
+    memcpy(d.M, g.world_to_index, sizeof(d.M));
+    d.root = (const int*)up(g.root_child.data(), g.root_child.size() * 4);
+    d.l1vmin = (const int4*)up(g.l1_vmin.data(), g.l1_vmin.size() * 4);
+    d.l1child = (const int*)up(g.l1_child.data(), g.l1_child.size() * 4);
+    d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
+    d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
+    if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
+    else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+    if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) { c->err = "out of device memory (temperature)"; return VR_ERR_OOM; }
+    float tab[384];
+    if (lut) memcpy(tab, lut, sizeof(tab));
+    else vr::blackbody_lut(tab);
+    memcpy(c->scene.blackbody, tab, sizeof(tab));
+    c->scene.leScale = le_scale;
+    c->scene.tCutoff = cutoff;
+    c->scene.tScale = scale;
+    c->scene.hasEmission = 1;
+    return VR_OK;
+}
+
 int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
     if (!c || !vol || !m) return VR_ERR_INVALID_ARG;
     if (!(m->sigma_s[0] + m->sigma_a[0] > 0.f)) { c->err = "sigma_t must be positive"; return VR_ERR_INVALID_ARG; }

@@ -166,6 +166,34 @@ std::vector<float> procedural_density(const vr_procedural_desc& d) {
     return g;
 }
 
+// Fire plume: a vertical column whose radius grows with height, fBm turbulence, density
+// falling off with height; the temperature follows the same turbulence, hottest at the base,
+// in [t_min, t_max] inside the plume and 0 outside.
+void procedural_fire(const vr_procedural_desc& d, float t_min, float t_max, std::vector<float>& density, std::vector<float>& temperature) {
+    const int R = d.res;
+    density.assign((size_t)R * R * R, 0.0f);
+    temperature.assign((size_t)R * R * R, 0.0f);
+    Perlin pn(d.seed);
+    const float inv = 1.0f / (float)R;
+    parallel_for(R, [&](int z) {
+        for (int y = 0; y < R; ++y)
+            for (int x = 0; x < R; ++x) {
+                float ux = ((float)x + 0.5f) * inv, uy = ((float)y + 0.5f) * inv, uz = ((float)z + 0.5f) * inv;
+                float n = pn.fbm(ux * d.base_frequency + 0.37f, uy * d.base_frequency * 0.7f + 1.91f,
+                                 uz * d.base_frequency + 4.13f, d.octaves, d.lacunarity, d.gain);
+                float dx = ux - 0.5f, dz = uz - 0.5f;
+                float dist = sqrt_(dx * dx + dz * dz);
+                float rad = 0.08f + 0.25f * uy + 0.05f * n;
+                float t = clamp01((rad - dist) / 0.06f) * clamp01((0.92f - uy) / 0.08f) * clamp01((uy - 0.02f) / 0.03f);
+                float env = t * t * (3.0f - 2.0f * t);
+                if (env <= 0.f) continue;
+                size_t i = ((size_t)z * R + y) * R + x;
+                density[i] = clamp01(0.6f + 0.8f * n) * env * exp_(-2.5f * uy);
+                temperature[i] = t_min + (t_max - t_min) * clamp01(0.75f + 0.9f * n) * clamp01(1.05f - 0.8f * uy);
+            }
+    });
+}
+
 // ---------------------------------------------------------------------------------------
 // mip pyramids (gvdb_volume_gvdb.cpp:2702-2862)
 // ---------------------------------------------------------------------------------------
@@ -366,6 +394,46 @@ void slot_view(const GridSlot& s, vr_grid_view* v) {
     v->brick_bounds = s.brick_bounds.data();
     v->brick_f32 = s.brick_f32.empty() ? nullptr : s.brick_f32.data();
     v->brick_f16 = s.brick_f16.empty() ? nullptr : s.brick_f16.data();
+}
+
+// ---------------------------------------------------------------------------------------
+// blackbody colour table for volume emission: Planck's law B(lambda, T) integrated over
+// 360..830 nm (1 nm steps) against the CIE 1931 colour-matching functions in the multi-lobe
+// Gaussian fit of Wyman, Sloan and Shirley ("Simple Analytic Approximations to the CIE XYZ
+// Color Matching Functions", JCGT 2013), then XYZ -> linear sRGB (D65) and normalised to unit
+// luminance at the last entry.  Entry i is T = 50 + 50 i kelvin (the texel centres of a
+// 128-texel table over [25, 6425) K).
+// ---------------------------------------------------------------------------------------
+static double lobe(double l, double mu, double s1, double s2) {
+    const double t = (l - mu) / (l < mu ? s1 : s2);
+    return std::exp(-0.5 * t * t);
+}
+void blackbody_lut(float rgb[384]) {
+    const double h = 6.62607015e-34, c = 2.99792458e8, kB = 1.380649e-23;
+    double X[128], Y[128], Z[128];
+    for (int i = 0; i < 128; ++i) {
+        const double T = 50.0 + 50.0 * i;
+        double x = 0, y = 0, z = 0;
+        for (int nm = 360; nm <= 830; ++nm) {
+            const double l = nm * 1e-9;
+            const double B = 2.0 * h * c * c / (l * l * l * l * l) / std::expm1(h * c / (l * kB * T));
+            const double xb = 1.056 * lobe(nm, 599.8, 37.9, 31.0) + 0.362 * lobe(nm, 442.0, 16.0, 26.7) - 0.065 * lobe(nm, 501.1, 20.4, 26.2);
+            const double yb = 0.821 * lobe(nm, 568.8, 46.9, 40.5) + 0.286 * lobe(nm, 530.9, 16.3, 31.1);
+            const double zb = 1.217 * lobe(nm, 437.0, 11.8, 36.0) + 0.681 * lobe(nm, 459.0, 26.0, 13.8);
+            x += B * xb; y += B * yb; z += B * zb;
+        }
+        X[i] = x; Y[i] = y; Z[i] = z;
+    }
+    const double norm = 1.0 / Y[127];
+    for (int i = 0; i < 128; ++i) {
+        const double x = X[i] * norm, y = Y[i] * norm, z = Z[i] * norm;
+        const double r = 3.2406 * x - 1.5372 * y - 0.4986 * z;
+        const double g = -0.9689 * x + 1.8758 * y + 0.0415 * z;
+        const double b = 0.0557 * x - 0.2040 * y + 1.0570 * z;
+        rgb[3 * i + 0] = (float)std::max(r, 0.0);
+        rgb[3 * i + 1] = (float)std::max(g, 0.0);
+        rgb[3 * i + 2] = (float)std::max(b, 0.0);
+    }
 }
 
 }  // namespace vr

@@ -76,6 +76,11 @@ struct DevScene {
     int impOff[12];
     int impDim, impBaseMip;
     int* status;                 // device status word (kStatus* bits)
+    // volume emission (VolumeBase.slang:196-232): temperature grid (mip 0), blackbody table
+    int hasEmission;
+    DevSlot tslot;
+    float leScale, tCutoff, tScale;
+    float blackbody[128][3];     // radiance of 50 K .. 6400 K in steps of 50 K (texel centres)
 };
 
 struct SamplingOptions {         // HostDeviceSharedDefinitions.h:96-141
@@ -309,6 +314,36 @@ static __device__ __noinline__ float densityWorld(f3 pw, int mip) {
     int br = findBrick(s, p, vmin);
     if (br < 0) return 0.f;
     return trilinearIn(s, br, p - vmin) * c_scene.dscale;
+}
+
+// Temperature / ConvertTempToColor / EmissionWorldSpace (VolumeBase.slang:196-232): trilinear
+// temperature at mip 0, mapped to a blackbody colour through the 128-texel table with linear
+// filtering between texel centres and clamped addressing
+static __device__ __noinline__ float temperatureWorld(f3 pw) {
+    const DevSlot& s = c_scene.tslot;
+    f3 p = mulPoint(pw, s.M);
+    if (p.x < 0.f || p.y < 0.f || p.z < 0.f || p.x >= s.bmaxf || p.y >= s.bmaxf || p.z >= s.bmaxf) return 0.f;
+    f3 vmin;
+    int br = findBrick(s, p, vmin);
+    if (br < 0) return 0.f;
+    return trilinearIn(s, br, p - vmin);
+}
+__device__ inline f3 tempToColor(float temp) {
+    temp = vr::fmin_(6400.f, (temp - c_scene.tCutoff) * c_scene.tScale);
+    const float q = (temp - 25.f) / 6400.f;
+    const float x = q * 128.f - 0.5f;
+    const float fl = vr::floor_(x);
+    const float f = x - fl;
+    int i0 = vr::f2i(fl), i1 = i0 + 1;
+    i0 = i0 < 0 ? 0 : (i0 > 127 ? 127 : i0);
+    i1 = i1 < 0 ? 0 : (i1 > 127 ? 127 : i1);
+    const f3 a = mk3(c_scene.blackbody[i0][0], c_scene.blackbody[i0][1], c_scene.blackbody[i0][2]);
+    const f3 b = mk3(c_scene.blackbody[i1][0], c_scene.blackbody[i1][1], c_scene.blackbody[i1][2]);
+    return c_scene.leScale * (a + (b - a) * f);
+}
+__device__ inline f3 emissionWorld(f3 pw) {
+    if (!c_scene.hasEmission) return mk3(0.f);
+    return tempToColor(temperatureWorld(pw));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1006,7 +1041,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
         if (isBg) {
             F = F * envEval(ray.d);
         } else if (isSelfEmission) {
-            F = F * mk3(0.f);
+            F = F * emissionWorld(pW);
         } else {
             bool scatterEm = false;
             Ray sr{};
@@ -1053,7 +1088,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
                     mi.p = pW;
                     if (vr::all_eq0(F)) return mk3(0.f);
                 }
-                if (scatterEm) F = F * mk3(0.f);
+                if (scatterEm) F = F * emissionWorld(pW);
                 else mi = MediumInteraction{at(sr, sr.tMax), -sr.d, c_scene.g, true};
             }
             if (!scatterEm && vr::any_gt0(F))

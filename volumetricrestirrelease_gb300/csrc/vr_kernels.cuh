@@ -93,6 +93,7 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
                 out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
                 float lightPdf = 0.f;
                 f3 Le = mk3(0.f);
+                if (c_scene.hasEmission && density > 0.f) Le = emissionWorld(mi.p);
                 f3 oma = mk3(1.f) - albedo;
                 f3 Ld = sampleDirectLighting(sg, lightPdf, mi, o, o.lightSamples != 0, out.lightID, out.uv0, out.uv1);
                 f3 wo = -ray.d, wi = mk3(0.f);
@@ -169,7 +170,7 @@ static __device__ __noinline__ f3 integratePT(const FrameParams& P, Ray ray, vr:
         if (mi.valid) {
             f3 albedo = c_scene.sigma_s / c_scene.sigma_t;
             f3 oma = mk3(1.f) - albedo;
-            { f3 Le = mk3(0.f); L = L + Le * oma * beta; }
+            { f3 Le = emissionWorld(mi.p); L = L + Le * oma * beta; }
             beta = beta * albedo;
             f3 Ld = mk3(0.f);
             for (int s = 0; s < lightSamples; s++) {

@@ -98,6 +98,7 @@ static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray r
                 out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
                 float lightPdf = 0.f;
                 f3 Le = mk3(0.f);
+                if (c_scene.hasEmission && density > 0.f) Le = emissionWorld(mi.p);
                 f3 oma = mk3(1.f) - albedo;
                 LightSample ls;
                 const bool lv = sampleLights(mi.p, o.useEnvironmentLights != 0, o.useAnalyticLights != 0, sg, ls, out.lightID, out.uv0, out.uv1);

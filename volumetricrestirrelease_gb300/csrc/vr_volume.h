@@ -35,6 +35,8 @@ std::vector<float> procedural_density(const vr_procedural_desc& d);
 int build_volume(const std::vector<float>& dense, int R, int numMips, const float wmin[3],
                  float vsize, bool fp16, Volume& vol);
 void slot_view(const GridSlot& s, vr_grid_view* v);
+void blackbody_lut(float rgb[384]);
+void procedural_fire(const vr_procedural_desc& d, float t_min, float t_max, std::vector<float>& density, std::vector<float>& temperature);
 
 }  // namespace vr
 

@@ -38,6 +38,16 @@ class Volume:
         return cls(h, lib)
 
     @classmethod
+    def fire(cls, desc, t_min, t_max, lib=None):
+        """Fire plume: (density volume, temperature volume)."""
+        lib = lib or capi.load()
+        hd, ht = C.c_void_p(), C.c_void_p()
+        r = lib.vr_volume_create_fire(C.byref(desc), t_min, t_max, C.byref(hd), C.byref(ht))
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_create_fire failed ({r})")
+        return cls(hd, lib), cls(ht, lib)
+
+    @classmethod
     def dense(cls, density, world_min, voxel_size, num_mips=4, fp16=False, lib=None):
         lib = lib or capi.load()
         d = np.ascontiguousarray(density, dtype=np.float32)
@@ -70,6 +80,14 @@ class Volume:
         if getattr(self, "_h", None):
             self._lib.vr_volume_destroy(self._h)
             self._h = None
+
+
+def blackbody_lut(lib=None):
+    """The library's blackbody table: (128, 3) linear sRGB for 50 K .. 6400 K."""
+    lib = lib or capi.load()
+    out = np.zeros(384, np.float32)
+    lib.vr_blackbody_lut(out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out.reshape(128, 3)
 
 
 def env_struct(rgb, scale=(1.0, 1.0, 1.0), rotation=None):
@@ -126,6 +144,16 @@ class VolumetricReSTIR:
         self._check(self._lib.vr_set_lights(self._h, arr, len(lights), C.byref(env) if env is not None else None))
 
     # ---- frames ----
+    def setEmission(self, temperature, le_scale, cutoff=0.0, scale=1.0, lut=None):
+        """Volume emission from a temperature volume (None switches it off)."""
+        self._temperature = temperature
+        lp = None
+        if lut is not None:
+            self._lut = np.ascontiguousarray(lut, np.float32).reshape(384)
+            lp = self._lut.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self._lib.vr_set_emission(self._h, temperature._h if temperature is not None else None, le_scale, cutoff,
+                                              scale, lp))
+
     def execute(self, camera, out_ptr, mvec_ptr=None, stream=0):
         """Renders one frame into device memory (width*height float4)."""
         self._check(self._lib.vr_render_frame(self._h, C.byref(camera), C.c_void_p(out_ptr),

@@ -14,6 +14,9 @@ stand in for them with the shapes, sizes and value ranges of the benchmark confi
            max path length 3, 32 candidates, temporal + 3 spatial neighbours; the camera
            orbits 0.5 deg per frame.
   small_fp16 : `small` with FP16 bricks.
+  fire   : 128^3 fire plume (fBm turbulence, density falling off with height) with a
+           temperature grid of 500..3000 K emitting blackbody radiance; sigma_t 30, albedo 0.6;
+           one point light + dim sky; max path length 3, 16 candidates, temporal + spatial.
 """
 import math
 from dataclasses import dataclass, field
@@ -39,6 +42,7 @@ class SceneDesc:
     orbit_deg_per_frame: float = 0.0
     fov_deg: float = 45.0
     frames: int = 16
+    fire: tuple = None             # (t_min, t_max, le_scale, cutoff, scale) for emissive plumes
 
     def camera(self, frame=0):
         ang = math.radians(self.orbit_deg_per_frame * frame)
@@ -146,4 +150,25 @@ def full(width=1920, height=1080, fp16=False):
         camera_radius=2.4, camera_height=0.3, orbit_deg_per_frame=0.5, frames=64)
 
 
-CONFIGS = {"small": small, "full": full, "small_fp16": lambda **k: small(fp16=True, **k)}
+def fire(width=256, height=256, fp16=False, res=128, seed=11):
+    light = capi.PointLight()
+    light.pos[:] = [2.0, 3.0, -2.0]
+    light.intensity[:] = [40.0, 40.0, 40.0]
+    vol = _procedural(2, res, 5, seed, 0.0, (-0.5, -0.5, -0.5), 1.0 / res, fp16=fp16, num_mips=3, base_frequency=5.0)
+    return SceneDesc(
+        name="fire_fp16" if fp16 else "fire", width=width, height=height, volume=vol,
+        medium=_medium(30.0, 0.6, 0.2), lights=[light], env_rgb=constant_env(0.05),
+        options=dict(mMaxBounces=3, mInitialM=16, mEnableTemporalReuse=1, mEnableSpatialReuse=1, mSpatialSampleCount=4,
+                     mSampleRadius=10.0, mUseAnalyticLights=1, mUseEnvironmentLights=1),
+        camera_radius=2.2, frames=16, fire=(500.0, 3000.0, 100.0, 0.0, 1.0))
+
+
+def make_volumes(sc, lib=None):
+    """(density volume, temperature volume or None) of a scene."""
+    from .restir import Volume
+    if sc.fire:
+        return Volume.fire(sc.volume, sc.fire[0], sc.fire[1], lib=lib)
+    return Volume.procedural(sc.volume, lib=lib), None
+
+
+CONFIGS = {"small": small, "full": full, "small_fp16": lambda **k: small(fp16=True, **k), "fire": fire}
