@@ -283,6 +283,33 @@ int vr_render_frame_host(vr_context* ctx, const vr_camera* cam, float* out_rgba_
 int vr_render_frame_noalloc(vr_context* ctx, const vr_camera* cam, int32_t frame_index,
                             float* out_rgba_device, void* stream);
 
+/* ---- batches (no counterpart in the reference) ----
+ * Many contexts -- each with its own volume, view, resolution, options, network and buffers --
+ * rendered together: every pass is one persistent launch over a single list of pixel tiles of
+ * all instances, and the whole launch sequence of a frame is captured once into a CUDA graph
+ * and replayed (re-captured when resolutions, buffers or the launch shape change).  Results are
+ * bit-identical to rendering each context alone with vr_render_frame.  All instances must share
+ * mMaxBounces, mEnableTemporalReuse, mEnableSpatialReuse and mSpatialReuseRounds, with
+ * mUseReference off.  The batch keeps pointers to the contexts; destroy it first. */
+typedef struct vr_batch vr_batch;
+int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out);
+void vr_batch_destroy(vr_batch* batch);
+const char* vr_batch_last_error(const vr_batch* batch);
+/* One frame of every instance: cams[i] and outs_device[i] (width_i*height_i float4). */
+int vr_batch_render(vr_batch* batch, const vr_camera* cams, float* const* outs_device, void* stream);
+int vr_batch_set_graph(vr_batch* batch, int32_t enable);            /* default on */
+/* Launch shape of the batched kernels: tiles of tile_w x (128 / tile_w) pixels, a persistent
+ * grid of blocks_per_sm blocks per SM. */
+int vr_batch_set_launch_shape(vr_batch* batch, int32_t tile_w, int32_t blocks_per_sm);
+int vr_batch_get_launch_shape(const vr_batch* batch, int32_t* tile_w, int32_t* tile_h, int32_t* blocks_per_sm);
+/* Autotuner: renders one real frame of the batch with each candidate launch shape (tiles 8x16,
+ * 16x8, 32x4 x 3, 5, 8 blocks per SM; at most max_trials of them when max_trials > 0), times it
+ * with CUDA events and keeps the fastest.  trial_ms (optional) receives the frame times. */
+int vr_batch_autotune(vr_batch* batch, const vr_camera* cams, float* const* outs_device, void* stream,
+                      float* trial_ms, int32_t max_trials);
+/* Kernel launches of the last batch frame (in the captured graph when it is on). */
+int32_t vr_batch_last_launch_count(const vr_batch* batch);
+
 /* ---- FP64 converged reference (IntegrateByVolumePathTracing,
  *      VolumePathTracingFunctions.slang:3-131, accumulated like AccumulatePass'
  *      accumulateDouble, Accumulate.cs.slang:100).  Renders num_frames frames of

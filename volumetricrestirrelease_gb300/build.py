@@ -21,7 +21,8 @@ LIB = PKG / "_lib" / "libvrestir.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                      "-ftz=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-v"]
-HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h", "vr_noalloc.h", "vr_lp.h", "vr_lp_kernels.cuh", "lp_net.h"]
+HEADERS = ["vr_math.h", "vr_device.cuh", "vr_kernels.cuh", "vr_volume.h", "vr_noalloc.h", "vr_lp.h", "vr_lp_kernels.cuh", "lp_net.h",
+           "vr_batch.h"]
 
 
 def _nvcc():
@@ -56,6 +57,10 @@ def build(force=False, jobs=None):
         obj = BUILD / f"frame_kernels_mb{mb}.o"
         src = CSRC / "frame_kernels.cu"
         units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-c", str(src), "-o", str(obj)]))
+    for mb in (1, 2, 3, 4):
+        obj = BUILD / f"batch_mb{mb}.o"
+        src = CSRC / "batch.cu"
+        units.append((obj, [src, CSRC / "vr_batch.h", CSRC / "vr_batch_kernels.cuh"] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-DVR_BATCHED", "-c", str(src), "-o", str(obj)]))
     obj = BUILD / "lp.o"
     src = CSRC / "lp.cu"
     units.append((obj, [src, CSRC / "umma.cuh"] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))

@@ -131,6 +131,15 @@ SIGNATURES = {
     "vr_selftest_math": (_i32, [_i32, C.POINTER(_f32), C.POINTER(_f32), C.POINTER(_f32), _i32]),
     "vr_selftest_rng": (_i32, [C.POINTER(_u32), _i32, _i32, C.POINTER(_f32)]),
     "vr_selftest_umma": (_i32, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(_f32), _i32]),
+    "vr_batch_create": (_i32, [C.POINTER(_P), _i32, C.POINTER(_P)]),
+    "vr_batch_destroy": (None, [_P]),
+    "vr_batch_last_error": (C.c_char_p, [_P]),
+    "vr_batch_render": (_i32, [_P, C.POINTER(Camera), C.POINTER(_P), _P]),
+    "vr_batch_set_graph": (_i32, [_P, _i32]),
+    "vr_batch_set_launch_shape": (_i32, [_P, _i32, _i32]),
+    "vr_batch_get_launch_shape": (_i32, [_P, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)]),
+    "vr_batch_autotune": (_i32, [_P, C.POINTER(Camera), C.POINTER(_P), _P, C.POINTER(_f32), _i32]),
+    "vr_batch_last_launch_count": (_i32, [_P]),
     "vr_net_get_params": (_i32, [_P, C.POINTER(_f32)]),
     "vr_net_set_params": (_i32, [_P, C.POINTER(_f32)]),
     "vr_net_infer": (_i32, [_P, _P, _i32, _P, _P]),

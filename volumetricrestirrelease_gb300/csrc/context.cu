@@ -40,8 +40,8 @@ VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 cudaError_t net_setup();
 void launch_net_infer(const vrd::NetView&, const float4*, int, const int*, float*, const int*, int*, int, cudaStream_t);
 void launch_net_train(const vrd::NetView&, const float4*, int, float*, float*, int*, cudaStream_t);
-void launch_net_reduce_adam(const float*, int, const float*, float*, float*, float*, float*, float*, uint16_t*, float*, float, float, float, int,
-                            cudaStream_t);
+void launch_net_reduce_adam(const float*, int, const float*, float*, float*, float*, float*, float*, uint16_t*, float*, float, float, float,
+                            const float*, int, cudaStream_t);
 void launch_net_pack(const float*, uint16_t*, float*, cudaStream_t);
 }
 
@@ -492,7 +492,7 @@ __global__ void k_gather_queries(const float4* __restrict__ q, const int* __rest
     out[2 * (size_t)i + 1] = q[2 * s + 1];
 }
 #endif
-static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st);
+static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st, const float* ccTable = nullptr);
 
 extern "C" {
 
@@ -1138,7 +1138,7 @@ static int net_grad_common(vr_context* c, const float* samples, int32_t n, float
     } else {
         vrk::launch_net_train(net_view(c), (const float4*)samples, n, c->netPart, c->netLossPart, c->status, 0);
         vrk::launch_net_reduce_adam(c->netPart, (n + 127) / 128, c->netLossPart, c->netW, c->netM, c->netV, c->netG, c->netScalar, c->netWbf,
-                                    c->netBias, 0.f, 1.f, 1.f, 0, 0);
+                                    c->netBias, 0.f, 1.f, 1.f, nullptr, 0, 0);
     }
     if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) return check_cuda(c, "network training");
     if (loss) cudaMemcpy(loss, update ? c->stepLoss : c->netScalar, sizeof(float), cudaMemcpyDeviceToHost);
@@ -1261,7 +1261,9 @@ static void launch_lp_train_gen(const vrd::FrameParams& P, const vrd::LpBuffers&
 static uint32_t lp_train_seed(uint32_t learnedSeed, int frameCount) { return 0x80000000u | ((learnedSeed * 0x9E3779B9u + (uint32_t)frameCount) & 0x7FFFFFFFu); }
 
 // one Adam step per batch over the frame's fresh training samples
-static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st) {
+// ccTable (device, optional): the bias corrections of each step, [steps][2], instead of
+// arguments computed here (graph replay)
+static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st, const float* ccTable) {
     const vr_options& o = c->opts;
     const int Bt = std::max(1, std::min(o.mLearnedBatch, S));
     const int steps = std::max(1, S / Bt);
@@ -1272,7 +1274,7 @@ static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStre
         const float c1 = (float)(1.0 - std::pow(0.9, (double)c->adamStep));
         const float c2 = (float)(1.0 - std::pow(0.999, (double)c->adamStep));
         vrk::launch_net_reduce_adam(c->netPart, (Bt + 127) / 128, c->netLossPart, c->netW, c->netM, c->netV, c->netG, c->stepLoss + k,
-                                    c->netWbf, c->netBias, o.mLearnedLearningRate, c1, c2, 1, st);
+                                    c->netWbf, c->netBias, o.mLearnedLearningRate, c1, c2, ccTable ? ccTable + 2 * k : nullptr, 1, st);
         c->launches += 2;
     }
     c->lastSteps = steps;
@@ -1536,3 +1538,388 @@ int noalloc_prepare(vr_context* c, const vr_camera* cam, int32_t frame_index, No
 }
 void noalloc_error(vr_context* c, const char* msg) { c->err = msg; }
 }  // namespace vrk
+
+// ---------------------------------------------------------------------------------------
+// batches: many contexts rendered together by the persistent batched kernels (batch.cu), with
+// the launch sequence captured once into a CUDA graph and an autotuned launch shape
+// ---------------------------------------------------------------------------------------
+#include "vr_batch.h"
+
+namespace vrk {
+#define VR_BDECL(MB)                                                                      \
+    void launch_batch_pass_##MB(const vrd::BatchLaunch&, int, int, cudaStream_t);       \
+    void launch_batch_train_gen_##MB(const vrd::BatchLaunch&, int, cudaStream_t);
+VR_BDECL(1) VR_BDECL(2) VR_BDECL(3) VR_BDECL(4)
+#undef VR_BDECL
+}  // namespace vrk
+
+struct vr_batch {
+    std::vector<vr_context*> ctx;
+    int MB = 0, temporal = 0, spatial = 0, rounds = 0;
+    int tileW = 8, tileH = 16, blocksPerSM = 5, numSMs = 1;
+    // device copy of the per-frame data (instances, scenes, Adam bias corrections) and its
+    // pinned staging buffer: one host-to-device copy per frame
+    unsigned char* dData = nullptr;
+    unsigned char* hStage = nullptr;
+    size_t dataBytes = 0;
+    cudaEvent_t frameDone = nullptr;
+    bool pendingFrame = false;
+    // graph
+    bool useGraph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int64_t> sig;
+    int launches = 0;
+    std::string err;
+    // per-frame host state
+    std::vector<CamFrame> cfs;
+    std::vector<int> steps;
+    std::vector<size_t> ccOff;
+};
+
+static void batch_drop_graph(vr_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->sig.clear();
+}
+
+template <int MB>
+static void batch_pass(const vrd::BatchLaunch& BL, int pass, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_pass_1(BL, pass, grid, st);
+    else if (MB == 2) vrk::launch_batch_pass_2(BL, pass, grid, st);
+    else if (MB == 3) vrk::launch_batch_pass_3(BL, pass, grid, st);
+    else vrk::launch_batch_pass_4(BL, pass, grid, st);
+}
+template <int MB>
+static void batch_train_gen(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_train_gen_1(BL, grid, st);
+    else if (MB == 2) vrk::launch_batch_train_gen_2(BL, grid, st);
+    else if (MB == 3) vrk::launch_batch_train_gen_3(BL, grid, st);
+    else vrk::launch_batch_train_gen_4(BL, grid, st);
+}
+
+// host side of a batch frame: prepares every context, fills the staging buffer and returns the
+// launch descriptor and the signature of the launch sequence (what a captured graph depends on)
+static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs, vrd::BatchLaunch& BL, std::vector<int64_t>& sig) {
+    const int n = (int)b->ctx.size();
+    if (b->pendingFrame) { cudaEventSynchronize(b->frameDone); b->pendingFrame = false; }
+    for (int i = 0; i < n; ++i) {
+        vr_context* c = b->ctx[i];
+        if (!outs[i]) { b->err = "null output buffer"; return VR_ERR_INVALID_ARG; }
+        int r = prepare_frame(c, &cams[i]);
+        if (r) { b->err = "instance " + std::to_string(i) + ": " + c->err; return r; }
+        if (c->opts.mMaxBounces != b->MB || c->opts.mEnableTemporalReuse != b->temporal || c->opts.mEnableSpatialReuse != b->spatial ||
+            (b->spatial && c->opts.mSpatialReuseRounds != b->rounds) || c->opts.mUseReference) {
+            b->err = "instance " + std::to_string(i) + ": options no longer match the batch";
+            return VR_ERR_STATE;
+        }
+    }
+    // staging layout: instances, scenes, Adam tables
+    b->steps.assign(n, 0);
+    b->ccOff.assign(n, 0);
+    size_t ccFloats = 0;
+    for (int i = 0; i < n; ++i) {
+        vr_context* c = b->ctx[i];
+        if (lp_active(c) && c->opts.mLearnedTrainSamples > 0) {
+            const int S = c->opts.mLearnedTrainSamples;
+            b->steps[i] = std::max(1, S / std::max(1, std::min(c->opts.mLearnedBatch, S)));
+            b->ccOff[i] = ccFloats;
+            ccFloats += 2 * (size_t)b->steps[i];
+        }
+    }
+    const size_t instBytes = sizeof(vrd::BatchInstance) * n, sceneBytes = sizeof(vrd::DevScene) * n;
+    const size_t need = instBytes + sceneBytes + ccFloats * sizeof(float);
+    if (need > b->dataBytes) {
+        batch_drop_graph(b);
+        cudaFree(b->dData);
+        cudaFreeHost(b->hStage);
+        b->dData = nullptr; b->hStage = nullptr; b->dataBytes = 0;
+        if (cudaMalloc(&b->dData, need) != cudaSuccess || cudaMallocHost(&b->hStage, need) != cudaSuccess) {
+            b->err = "out of memory (batch descriptors)";
+            return VR_ERR_OOM;
+        }
+        b->dataBytes = need;
+    }
+    vrd::BatchInstance* hInst = (vrd::BatchInstance*)b->hStage;
+    vrd::DevScene* hScene = (vrd::DevScene*)(b->hStage + instBytes);
+    float* hCC = (float*)(b->hStage + instBytes + sceneBytes);
+    const vrd::DevScene* dScene = (const vrd::DevScene*)(b->dData + instBytes);
+    b->cfs.resize(n);
+    int tiles = 0, chunks = 0;
+    sig.clear();
+    sig.push_back(n); sig.push_back(b->tileW); sig.push_back(b->blocksPerSM); sig.push_back((int64_t)(size_t)b->dData);
+    for (int i = 0; i < n; ++i) {
+        vr_context* c = b->ctx[i];
+        const vr_options& o = c->opts;
+        vrd::BatchInstance& I = hInst[i];
+        memset(&I, 0, sizeof(I));
+        const CamFrame cf = camera_frame(cams[i], c->W, c->H);
+        b->cfs[i] = cf;
+        const int numTotalRounds = (o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0) + o.mEnableTemporalReuse + 1 + 1;
+        I.P = frame_params(c, cf, numTotalRounds);
+        I.B.cur = c->res[0]; I.B.sp[0] = c->res[0]; I.B.sp[1] = c->res[1]; I.B.hist = c->res[2];
+        I.B.featCur = c->feat[c->featCurIdx];
+        I.B.featPrev = c->feat[c->featCurIdx ^ 1];
+        I.B.color = nullptr;
+        I.B.out = (float4*)outs[i];
+        I.B.mvec = nullptr;
+        I.learned = lp_active(c) ? 1 : 0;
+        if (I.learned) {
+            c->lp.targetMethod = o.mLearnedTargetMethod;
+            I.L = c->lp;
+            I.trainSeed = lp_train_seed(o.mLearnedSeed, c->frameCount);
+        }
+        I.spatialRounds = o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0;
+        int totalRoundId = 0;
+        for (int r = 0; r < I.spatialRounds; ++r) {
+            vrd::SpatialParams& S = I.S[r];
+            S.in = totalRoundId % 2;
+            S.out = (totalRoundId + 1) % 2;
+            const int roundOffset = o.mEnableTemporalReuse + 1;
+            S.roundId = r;
+            S.numRounds = o.mSpatialReuseRounds + roundOffset + 1;
+            S.rid = r + roundOffset;
+            S.last = r == o.mSpatialReuseRounds - 1;
+            S.writeHistory = o.mEnableTemporalReuse;
+            neighbor_offsets(o, ((o.mSpatialReuseRounds + 1) * c->frameCount + r) % 16, S.offs);
+            totalRoundId++;
+        }
+        I.scene = dScene + i;
+        hScene[i] = c->scene;
+        I.tilesX = (c->W + b->tileW - 1) / b->tileW;
+        I.tileStart = tiles;
+        tiles += I.tilesX * ((c->H + b->tileH - 1) / b->tileH);
+        I.trainChunkStart = chunks;
+        if (I.learned && o.mLearnedTrainSamples > 0) chunks += (o.mLearnedTrainSamples + 127) / 128;
+        for (int k = 0; k < b->steps[i]; ++k) {
+            const double t = (double)(c->adamStep + k + 1);
+            hCC[b->ccOff[i] + 2 * k] = (float)(1.0 - std::pow(0.9, t));
+            hCC[b->ccOff[i] + 2 * k + 1] = (float)(1.0 - std::pow(0.999, t));
+        }
+        const int64_t s[] = {c->W, c->H, o.mInitialM, I.learned, I.spatialRounds, o.mLearnedTrainSamples, o.mLearnedBatch, b->steps[i],
+                             (int64_t)(size_t)c->res[0].a, (int64_t)(size_t)c->lp.vrecA, (int64_t)(size_t)c->lp.train,
+                             (int64_t)(size_t)c->netW, (int64_t)(size_t)c->netPart};
+        sig.insert(sig.end(), s, s + sizeof(s) / sizeof(s[0]));
+    }
+    BL.inst = (const vrd::BatchInstance*)b->dData;
+    BL.numInst = n;
+    BL.totalTiles = tiles;
+    BL.tileW = b->tileW;
+    BL.tileH = b->tileH;
+    BL.round = 0;
+    BL.trainChunks = chunks;
+    return VR_OK;
+}
+
+template <int MB>
+static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
+    const int n = (int)b->ctx.size();
+    const size_t instBytes = sizeof(vrd::BatchInstance) * n, sceneBytes = sizeof(vrd::DevScene) * n;
+    cudaMemcpyAsync(b->dData, b->hStage, b->dataBytes, cudaMemcpyHostToDevice, st);
+    const float* dCC = (const float*)(b->dData + instBytes + sceneBytes);
+    const int grid = std::max(1, b->numSMs * b->blocksPerSM);
+    bool anyPlain = false, anyLearned = false, anyTrain = false;
+    for (vr_context* c : b->ctx) {
+        if (lp_active(c)) { anyLearned = true; anyTrain |= c->opts.mLearnedTrainSamples > 0; }
+        else anyPlain = true;
+    }
+    int launches = 0;
+    if (anyPlain) { batch_pass<MB>(BL, 0, grid, st); launches++; }
+    if (anyLearned) {
+        for (vr_context* c : b->ctx)
+            if (lp_active(c)) cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+        batch_pass<MB>(BL, 1, grid, st);
+        launches++;
+        for (vr_context* c : b->ctx)
+            if (lp_active(c)) {
+                vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
+                launches++;
+            }
+        batch_pass<MB>(BL, 2, grid, st);
+        launches++;
+    }
+    if (b->temporal && !b->spatial) {
+        for (vr_context* c : b->ctx) {
+            const size_t N = (size_t)c->W * c->H;
+            cudaMemcpyAsync(c->res[2].a, c->res[0].a, N * 16, cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(c->res[2].b, c->res[0].b, N * 16, cudaMemcpyDeviceToDevice, st);
+            if (MB > 1) cudaMemcpyAsync(c->res[2].extra, c->res[0].extra, N * (size_t)(MB - 1) * 16, cudaMemcpyDeviceToDevice, st);
+        }
+    }
+    if (b->spatial) {
+        for (int r = 0; r < b->rounds; ++r) {
+            BL.round = r;
+            batch_pass<MB>(BL, 3, grid, st);
+            launches++;
+        }
+    } else {
+        batch_pass<MB>(BL, 4, grid, st);
+        launches++;
+    }
+    if (anyTrain) {
+        batch_train_gen<MB>(BL, grid, st);
+        launches++;
+        for (int i = 0; i < n; ++i) {
+            vr_context* c = b->ctx[i];
+            if (!lp_active(c) || c->opts.mLearnedTrainSamples <= 0) continue;
+            const int64_t step0 = c->adamStep;
+            lp_train_steps(c, c->lp.train, c->opts.mLearnedTrainSamples, st, dCC + b->ccOff[i]);
+            c->adamStep = step0;         // advanced once per frame in batch_finish (graph replays too)
+            launches += 2 * b->steps[i];
+        }
+    }
+    b->launches = launches;
+}
+
+static void batch_finish(vr_batch* b, cudaStream_t st) {
+    for (size_t i = 0; i < b->ctx.size(); ++i) {
+        vr_context* c = b->ctx[i];
+        const vr_options& o = c->opts;
+        if (o.mEnableTemporalReuse) c->featCurIdx ^= 1;
+        c->temporalSampleAccumulated = 1;
+        c->prev = b->cfs[i];
+        c->frameCount++;
+        c->finalBuf = (o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0) % 2;
+        c->launches = 0;
+        if (lp_active(c)) {
+            c->lpFrameDone = true;
+            c->adamStep += b->steps[i];
+            c->lastSteps = b->steps[i];
+        }
+    }
+    cudaEventRecord(b->frameDone, st);
+    b->pendingFrame = true;
+}
+
+static int batch_frame(vr_batch* b, const vr_camera* cams, float* const* outs, cudaStream_t st) {
+    vrd::BatchLaunch BL;
+    std::vector<int64_t> sig;
+    int r = batch_prepare(b, cams, outs, BL, sig);
+    if (r) return r;
+    auto launch = [&]() {
+        switch (b->MB) {
+            case 1: batch_launch<1>(b, BL, st); break;
+            case 2: batch_launch<2>(b, BL, st); break;
+            case 3: batch_launch<3>(b, BL, st); break;
+            default: batch_launch<4>(b, BL, st); break;
+        }
+    };
+    if (!b->useGraph) {
+        launch();
+    } else {
+        if (!b->exec || sig != b->sig) {
+            batch_drop_graph(b);
+            if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { b->err = "stream capture failed"; return VR_ERR_CUDA; }
+            launch();
+            if (cudaStreamEndCapture(st, &b->graph) != cudaSuccess || !b->graph) { b->err = "stream capture failed"; batch_drop_graph(b); return VR_ERR_CUDA; }
+            if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) { b->err = "graph instantiation failed"; batch_drop_graph(b); return VR_ERR_CUDA; }
+            b->sig = sig;
+        }
+        if (cudaGraphLaunch(b->exec, st) != cudaSuccess) { b->err = "graph launch failed"; return VR_ERR_CUDA; }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { b->err = std::string("batch frame: ") + cudaGetErrorString(e); return VR_ERR_CUDA; }
+    batch_finish(b, st);
+    return VR_OK;
+}
+
+extern "C" {
+
+int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
+    if (!ctxs || !out || n < 1 || n > 1024) return VR_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) if (!ctxs[i]) return VR_ERR_INVALID_ARG;
+    const vr_options& o0 = ctxs[0]->opts;
+    if (o0.mUseReference) return VR_ERR_INVALID_ARG;
+    for (int i = 1; i < n; ++i) {
+        const vr_options& o = ctxs[i]->opts;
+        if (o.mMaxBounces != o0.mMaxBounces || o.mEnableTemporalReuse != o0.mEnableTemporalReuse || o.mEnableSpatialReuse != o0.mEnableSpatialReuse ||
+            (o0.mEnableSpatialReuse && o.mSpatialReuseRounds != o0.mSpatialReuseRounds) || o.mUseReference)
+            return VR_ERR_INVALID_ARG;
+    }
+    vr_batch* b = new vr_batch();
+    b->ctx.assign(ctxs, ctxs + n);
+    b->MB = o0.mMaxBounces;
+    b->temporal = o0.mEnableTemporalReuse;
+    b->spatial = o0.mEnableSpatialReuse;
+    b->rounds = o0.mEnableSpatialReuse ? o0.mSpatialReuseRounds : 0;
+    cudaDeviceGetAttribute(&b->numSMs, cudaDevAttrMultiProcessorCount, 0);
+    if (b->numSMs <= 0) b->numSMs = 1;
+    cudaEventCreateWithFlags(&b->frameDone, cudaEventDisableTiming);
+    *out = b;
+    return VR_OK;
+}
+
+void vr_batch_destroy(vr_batch* b) {
+    if (!b) return;
+    if (b->pendingFrame) cudaEventSynchronize(b->frameDone);
+    batch_drop_graph(b);
+    cudaFree(b->dData);
+    cudaFreeHost(b->hStage);
+    if (b->frameDone) cudaEventDestroy(b->frameDone);
+    delete b;
+}
+
+const char* vr_batch_last_error(const vr_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+int vr_batch_set_graph(vr_batch* b, int32_t enable) {
+    if (!b) return VR_ERR_INVALID_ARG;
+    b->useGraph = enable != 0;
+    if (!b->useGraph) batch_drop_graph(b);
+    return VR_OK;
+}
+
+int vr_batch_set_launch_shape(vr_batch* b, int32_t tile_w, int32_t blocks_per_sm) {
+    if (!b || (tile_w != 4 && tile_w != 8 && tile_w != 16 && tile_w != 32) || blocks_per_sm < 1 || blocks_per_sm > 32) return VR_ERR_INVALID_ARG;
+    b->tileW = tile_w;
+    b->tileH = 128 / tile_w;
+    b->blocksPerSM = blocks_per_sm;
+    return VR_OK;
+}
+
+int vr_batch_get_launch_shape(const vr_batch* b, int32_t* tile_w, int32_t* tile_h, int32_t* blocks_per_sm) {
+    if (!b || !tile_w || !tile_h || !blocks_per_sm) return VR_ERR_INVALID_ARG;
+    *tile_w = b->tileW; *tile_h = b->tileH; *blocks_per_sm = b->blocksPerSM;
+    return VR_OK;
+}
+
+int vr_batch_render(vr_batch* b, const vr_camera* cams, float* const* outs, void* stream) {
+    if (!b || !cams || !outs) return VR_ERR_INVALID_ARG;
+    return batch_frame(b, cams, outs, (cudaStream_t)stream);
+}
+
+int32_t vr_batch_last_launch_count(const vr_batch* b) { return b ? b->launches : 0; }
+
+int vr_batch_autotune(vr_batch* b, const vr_camera* cams, float* const* outs, void* stream, float* trial_ms, int32_t max_trials) {
+    if (!b || !cams || !outs) return VR_ERR_INVALID_ARG;
+    static const int shapes[][2] = {{8, 5}, {16, 5}, {32, 5}, {8, 3}, {16, 3}, {32, 3}, {8, 8}, {16, 8}, {32, 8}};
+    const int nShapes = (int)(sizeof(shapes) / sizeof(shapes[0]));
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool graph = b->useGraph;
+    b->useGraph = false;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int bestK = 0, r = VR_OK;
+    for (int k = 0; k < nShapes && (max_trials <= 0 || k < max_trials); ++k) {
+        b->tileW = shapes[k][0]; b->tileH = 128 / shapes[k][0]; b->blocksPerSM = shapes[k][1];
+        cudaEventRecord(e0, st);
+        if ((r = batch_frame(b, cams, outs, st))) break;
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (trial_ms) trial_ms[k] = ms;
+        if (ms < best) { best = ms; bestK = k; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->tileW = shapes[bestK][0]; b->tileH = 128 / shapes[bestK][0]; b->blocksPerSM = shapes[bestK][1];
+    b->useGraph = graph;
+    batch_drop_graph(b);
+    return r;
+}
+
+}  // extern "C"

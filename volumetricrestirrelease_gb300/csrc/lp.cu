@@ -463,11 +463,15 @@ __device__ __forceinline__ void scatter_param(int i, float wi, uint16_t* wbf, fl
 }
 
 // sums the CTAs' partial gradients in a fixed order, then (update != 0) one Adam step
-// (beta1 0.9, beta2 0.999, eps 1e-8) on the FP32 master weights, refreshing the BF16 copy
+// (beta1 0.9, beta2 0.999, eps 1e-8) on the FP32 master weights, refreshing the BF16 copy; the
+// bias corrections c1 = 1 - 0.9^t, c2 = 1 - 0.999^t come as arguments or, when cc is not null,
+// from device memory (cc[0], cc[1]) so that a captured graph can replay the step
 __global__ void k_net_reduce_adam(const float* __restrict__ partials, int parts, const float* __restrict__ lossParts, float* __restrict__ w,
                                   float* __restrict__ m, float* __restrict__ v, float* __restrict__ grads, float* __restrict__ loss,
-                                  uint16_t* __restrict__ wbf, float* __restrict__ bias, float lr, float c1, float c2, int update) {
+                                  uint16_t* __restrict__ wbf, float* __restrict__ bias, float lr, float c1, float c2, const float* cc,
+                                  int update) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cc) { c1 = cc[0]; c2 = cc[1]; }
     if (i == 0) {
         float ls = 0.f;
         for (int p = 0; p < parts; ++p) ls += lossParts[p];
@@ -519,9 +523,9 @@ void launch_net_train(const vrd::NetView& net, const float4* samples, int n, flo
 }
 
 void launch_net_reduce_adam(const float* partials, int parts, const float* lossParts, float* w, float* m, float* v, float* grads, float* loss,
-                            uint16_t* wbf, float* bias, float lr, float c1, float c2, int update, cudaStream_t st) {
+                            uint16_t* wbf, float* bias, float lr, float c1, float c2, const float* cc, int update, cudaStream_t st) {
     lpk::k_net_reduce_adam<<<(lpn::kParams + 255) / 256, 256, 0, st>>>(partials, parts, lossParts, w, m, v, grads, loss, wbf, bias, lr, c1, c2,
-                                                                         update);
+                                                                         cc, update);
 }
 
 void launch_net_pack(const float* w, uint16_t* wbf, float* bias, cudaStream_t st) {

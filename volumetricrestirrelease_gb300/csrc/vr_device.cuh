@@ -119,8 +119,16 @@ struct ResBuf {
 };
 
 // Each translation unit that includes this header has its own copy of the scene constants
-// (internal linkage); the host uploads the same DevScene to every copy.
+// (internal linkage); the host uploads the same DevScene to every copy.  The batched kernels
+// (many scenes in one launch) keep the scene of the tile being processed in shared memory
+// instead: each block loads it from the instance's DevScene in global memory.
+#if defined(VR_BATCHED) && defined(VR_HOST_EMULATION)
+static thread_local DevScene c_scene;
+#elif defined(VR_BATCHED)
+static __shared__ DevScene c_scene;
+#else
 static __constant__ DevScene c_scene;
+#endif
 
 // ---------------------------------------------------------------------------------------
 // reservoir (Reservoir.slang); extraBounceStartId is carried as the owning pixel

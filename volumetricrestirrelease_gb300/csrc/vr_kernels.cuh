@@ -330,10 +330,7 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
 #define VR_KSPAT_MIN_BLOCKS 5
 #endif
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const FrameParams P, const FrameBuffers B) {
-    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
-    if (px >= P.W || py >= P.H) return;
+__device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBuffers& B, int px, int py) {
     const int W = P.W, H = P.H, N = P.N;
     const int pid = py * W + px;
     const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H));
@@ -382,6 +379,13 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const Fram
     }
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const FrameParams P, const FrameBuffers B) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    initialPixel<MB>(P, B, px, py);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -435,10 +439,7 @@ struct SpatialParams {
 };
 
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const FrameParams P, const FrameBuffers B, const SpatialParams S) {
-    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
-    if (px >= P.W || py >= P.H) return;
+__device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBuffers& B, const SpatialParams& S, int px, int py) {
     const int W = P.W, H = P.H, N = P.N;
     const int pid = py * W + px;
     const ResBuf& in = B.sp[S.in];
@@ -503,17 +504,28 @@ __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const Fram
         finalShade<MB>(P, B, outb, result, px, py);
     }
 }
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const FrameParams P, const FrameBuffers B, const SpatialParams S) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    spatialPixel<MB>(P, B, S, px, py);
+}
 
 // k_final: FinalShading without spatial reuse (optionally after the history copy)
+template <int MB>
+__device__ __forceinline__ void finalPixel(const FrameParams& P, const FrameBuffers& B, int writeHist, int px, int py) {
+    const int pid = py * P.W + px;
+    Reservoir r = loadRes(B.cur, pid);
+    if (writeHist) writeHistory<MB>(B, B.cur, r, pid, P.N);
+    finalShade<MB>(P, B, B.cur, r, px, py);
+}
 template <int MB>
 __global__ void __launch_bounds__(128) k_final(const FrameParams P, const FrameBuffers B, int writeHist) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
-    const int pid = py * P.W + px;
-    Reservoir r = loadRes(B.cur, pid);
-    if (writeHist) writeHistory<MB>(B, B.cur, r, pid, P.N);
-    finalShade<MB>(P, B, B.cur, r, px, py);
+    finalPixel<MB>(P, B, writeHist, px, py);
 }
 
 // k_reference: FP64 accumulation of the path tracer over frames [first, first + count)

@@ -179,10 +179,7 @@ static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray r
 
 // generate: GenerateFeatures + the candidates of TraceRays, recorded
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
-    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
-    if (px >= P.W || py >= P.H) return;
+__device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
     const int W = P.W, H = P.H, N = P.N;
     const int pid = py * W + px;
     const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H));
@@ -205,14 +202,18 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const 
     L.rng[pid] = make_uint4(sg.s[0], sg.s[1], sg.s[2], sg.s[3]);
     (void)H;
 }
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    lpGeneratePixel<MB>(P, B, L, px, py);
+}
 
 // select: resample the recorded candidates with the predicted transmittance, then finish
 // TraceRays (p_hat of the winner) and run TemporalReuse as k_initial does
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
-    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
-    if (px >= P.W || py >= P.H) return;
+__device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
     const int W = P.W, N = P.N;
     const int pid = py * W + px;
     const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, P.H));
@@ -265,6 +266,13 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const Fr
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+    const int px = blockIdx.x * 8 + (threadIdx.x & 7);
+    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    if (px >= P.W || py >= P.H) return;
+    lpSelectPixel<MB>(P, B, L, px, py);
+}
 
 // training samples of the network, drawn from the queries the frame's candidates made: sample i
 // picks a pixel and a starting slot from its own stream and takes the first slot of that pixel
@@ -272,9 +280,7 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const Fr
 // trilinear) estimate of the transmittance of the query's shadow ray, by ray marching (default) or
 // by (residual) ratio tracking.  A sample that found no query is invalid (tmax = -1).
 template <int MB>
-__global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const LpBuffers L, uint32_t seed) {
-    const int i = blockIdx.x * 128 + threadIdx.x;
-    if (i >= L.trainCount) return;
+__device__ __forceinline__ void lpTrainSample(const FrameParams& P, const LpBuffers& L, uint32_t seed, int i) {
     const int N = P.N, S = L.numSlots;
     vr::Rng sg = vr::rng_create((uint32_t)i & 0x3FFFu, (uint32_t)i >> 14, seed);
     int slot = -1;
@@ -297,6 +303,12 @@ __global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const
     }
     L.train[2 * (size_t)i] = a;
     L.train[2 * (size_t)i + 1] = b;
+}
+template <int MB>
+__global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const LpBuffers L, uint32_t seed) {
+    const int i = blockIdx.x * 128 + threadIdx.x;
+    if (i >= L.trainCount) return;
+    lpTrainSample<MB>(P, L, seed, i);
 }
 
 }  // namespace vrd

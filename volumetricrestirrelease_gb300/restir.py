@@ -270,6 +270,59 @@ class VolumetricReSTIR:
             self._h = None
 
 
+class Batch:
+    """Many VolumetricReSTIR instances rendered by persistent batched launches (and a CUDA graph)."""
+
+    def __init__(self, renderers, graph=True):
+        self._r = list(renderers)
+        self._lib = self._r[0]._lib
+        arr = (C.c_void_p * len(self._r))(*[r._h for r in self._r])
+        h = C.c_void_p()
+        rc = self._lib.vr_batch_create(arr, len(self._r), C.byref(h))
+        if rc != capi.VR_OK:
+            raise RuntimeError(f"vr_batch_create failed ({rc})")
+        self._h = h
+        self._lib.vr_batch_set_graph(self._h, 1 if graph else 0)
+
+    def _args(self, cams, out_ptrs):
+        ca = (capi.Camera * len(cams))(*cams)
+        oa = (C.c_void_p * len(out_ptrs))(*out_ptrs)
+        return ca, oa
+
+    def render(self, cams, out_ptrs, stream=0):
+        ca, oa = self._args(cams, out_ptrs)
+        self._check(self._lib.vr_batch_render(self._h, ca, oa, C.c_void_p(stream)))
+
+    def autotune(self, cams, out_ptrs, stream=0, max_trials=0):
+        ca, oa = self._args(cams, out_ptrs)
+        ms = (C.c_float * 16)()
+        self._check(self._lib.vr_batch_autotune(self._h, ca, oa, C.c_void_p(stream), ms, max_trials))
+        return list(ms[: (max_trials or 9)]), self.launch_shape()
+
+    def set_launch_shape(self, tile_w, blocks_per_sm):
+        self._check(self._lib.vr_batch_set_launch_shape(self._h, tile_w, blocks_per_sm))
+
+    def launch_shape(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._lib.vr_batch_get_launch_shape(self._h, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value
+
+    def last_launch_count(self):
+        return self._lib.vr_batch_last_launch_count(self._h)
+
+    def set_graph(self, on):
+        self._lib.vr_batch_set_graph(self._h, 1 if on else 0)
+
+    def _check(self, r):
+        if r != capi.VR_OK:
+            raise RuntimeError(f"libvrestir batch error {r}: {self._lib.vr_batch_last_error(self._h).decode()}")
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.vr_batch_destroy(self._h)
+            self._h = None
+
+
 RESERVOIR_DTYPE_36 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
                                ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4"),
                                ("extraBounceStartId", "<i4")])
