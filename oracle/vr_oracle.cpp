@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <cstdio>
 #include <thread>
 #include <vector>
 
@@ -447,6 +448,12 @@ static void VolumeTrackingGVDB(const Scene& sc, const Ray& rWorld, int mipLevel,
             if (lev == 1) {
                 nodeid[0] = child;
                 t = dda.t.x - epsilon;
+                // Deviation from VolumeUtils.slang:240-249: stop when the next occupied brick
+                // starts beyond tFar.  The reference enters it with t > tFar, and the analytic
+                // and residual-ratio adapters then integrate over a negative interval
+                // (t_dist = tFar - t < 0), returning transmittances far above 1 (up to e^60
+                // observed: fireflies of 1e26 in the final shading).
+                if (t >= tFar) break;
                 f3 vmin_leaf = nodeVmin(s, 0, child);
                 float bnd[4];
                 for (int k = 0; k < 4; ++k) bnd[k] = s.bounds[(size_t)child * 4 + k] * sc.med.dscale;
@@ -2637,6 +2644,27 @@ void vro_net_forward(const float* params, const float bmin[3], const float binv[
 void vro_net_gradients(const float* params, const float bmin[3], const float binv[3], const float* samples, int n, int lossLog, float floor_,
                        float* grads, float* loss) {
     oracle::lpo::gradients(params, samples, n, bmin, binv, lossLog, floor_, grads, loss);
+}
+
+// debugging aid: F of one reservoir (with its suffix records) at pixel (px, py), final options
+int vro_eval_F(void* h, const vr_camera* camIn, const vr_reservoir_aos* ra, const float* extra, int px, int py, int frameCount, float out[3]) {
+    Oracle* p = (Oracle*)h;
+    oracle::Ctx c;
+    p->makeOptions(c);
+    oracle::CamFrame cam = oracle::makeCamera(*camIn, p->W, p->H);
+    const int numTotalRounds = (p->opts.mEnableSpatialReuse ? p->opts.mSpatialReuseRounds : 0) + p->opts.mEnableTemporalReuse + 1 + 1;
+    Rng sg = rng_create((uint32_t)px, (uint32_t)py, (uint32_t)(numTotalRounds * frameCount + numTotalRounds - 1));
+    oracle::Reservoir r;
+    r.runningSum = ra->runningSum; r.M = ra->M; r.depth = ra->depth; r.p_y = ra->p_y;
+    r.lightUV[0] = ra->lightUV[0]; r.lightUV[1] = ra->lightUV[1]; r.lightID = ra->lightID; r.sampledPixel = ra->sampledPixel;
+    r.extraBounceStartId = 0;
+    std::vector<f3> ex(4);
+    for (int b = 0; b < 3; ++b) ex[b] = mk3(extra[3 * b], extra[3 * b + 1], extra[3 * b + 2]);
+    oracle::ExtraProvider prov{ex.data()};
+    oracle::Ray ray{cam.posW, normalize(oracle::rayDirPinhole(cam, px, py, p->W, p->H)), 0, r.depth};
+    f3 col = oracle::evaluate_F_(c, r, prov, ray, sg, c.fin, c.noReuse, true);
+    out[0] = col.x; out[1] = col.y; out[2] = col.z;
+    return 0;
 }
 
 }  // extern "C"

@@ -106,3 +106,34 @@ def test_density_lookup_trilinear(homogeneous):
     assert o.L.vro_density_world(o._h, p, 0) == pytest.approx(0.5, abs=1e-7)
     p = (C.c_float * 3)(5.0, 0.0, 0.0)
     assert o.L.vro_density_world(o._h, p, 0) == 0.0
+
+
+@pytest.mark.parametrize("method,linear", [(capi.VR_TRACK_ANALYTIC, 1), (capi.VR_TRACK_ANALYTIC, 0), (capi.VR_TRACK_RESIDUAL_RATIO, 1),
+                                           (capi.VR_TRACK_RAY_MARCHING, 1)])
+def test_segment_ending_before_the_next_brick(vlib, method, linear):
+    """A shadow segment that ends in empty space before the next occupied brick: the tracker
+    must stop at the segment's end (the reference's traversal enters the next brick with
+    t > tFar and its analytic / residual-ratio adapters then integrate over a negative
+    interval, returning T far above 1)."""
+    from oracle.oracle import Oracle
+    g = np.zeros((64, 64, 64), np.float32)
+    g[:, :, 8:16] = 0.5            # first occupied slab of bricks along x (arrays are [z][y][x])
+    g[:, :, 40:48] = 0.9           # second slab, beyond the segment's end
+    vol = Volume.dense(g, (0.0, 0.0, 0.0), 1.0 / 64, num_mips=1, lib=vlib)
+    m = capi.Medium()
+    m.sigma_s[:] = [SIGMA_T * 0.8] * 3
+    m.sigma_a[:] = [SIGMA_T - SIGMA_T * 0.8] * 3
+    m.g = 0.0
+    m.density_scale = 1.0
+    o = Oracle(8, 8, capi.default_options(vlib))
+    o.set_volume(vol, m)
+    d = np.array([1.0, 0.013, 0.007])
+    d /= np.linalg.norm(d)
+    origin = (9.3 / 64, 30.1 / 64, 31.7 / 64)
+    tmax = (30.0 - 9.3) / 64 / d[0]          # ends at x = 30 voxels, in the gap
+    ts = [_tr(o, origin, tuple(d), tmax, method, linear=linear, seed=s) for s in range(1, 33)]
+    if method != capi.VR_TRACK_RESIDUAL_RATIO:        # single ratio-tracking estimates may exceed 1
+        for t in ts:
+            assert 0.0 <= t <= 1.0 + 1e-6, t
+    # about 6.7 voxels of density 0.5 (sigma_t 3, voxel 1/64) lie on the segment
+    assert np.mean(ts) == pytest.approx(math.exp(-SIGMA_T * 0.5 * (16 - 9.3) / 64 / d[0]), rel=0.15)

@@ -1564,6 +1564,10 @@ struct vr_batch {
     size_t dataBytes = 0;
     cudaEvent_t frameDone = nullptr;
     bool pendingFrame = false;
+    // the graph is captured on and launched into a stream of its own, ordered after and before
+    // the caller's stream by events (the legacy default stream cannot be captured)
+    cudaStream_t gstream = nullptr;
+    cudaEvent_t evIn = nullptr, evOut = nullptr;
     // graph
     bool useGraph = true;
     cudaGraph_t graph = nullptr;
@@ -1809,6 +1813,10 @@ static int batch_frame(vr_batch* b, const vr_camera* cams, float* const* outs, c
     if (!b->useGraph) {
         launch();
     } else {
+        const cudaStream_t user = st;
+        cudaEventRecord(b->evIn, user);
+        cudaStreamWaitEvent(b->gstream, b->evIn, 0);
+        st = b->gstream;
         if (!b->exec || sig != b->sig) {
             batch_drop_graph(b);
             if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { b->err = "stream capture failed"; return VR_ERR_CUDA; }
@@ -1818,6 +1826,9 @@ static int batch_frame(vr_batch* b, const vr_camera* cams, float* const* outs, c
             b->sig = sig;
         }
         if (cudaGraphLaunch(b->exec, st) != cudaSuccess) { b->err = "graph launch failed"; return VR_ERR_CUDA; }
+        cudaEventRecord(b->evOut, st);
+        cudaStreamWaitEvent(user, b->evOut, 0);
+        st = user;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) { b->err = std::string("batch frame: ") + cudaGetErrorString(e); return VR_ERR_CUDA; }
@@ -1847,6 +1858,9 @@ int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
     cudaDeviceGetAttribute(&b->numSMs, cudaDevAttrMultiProcessorCount, 0);
     if (b->numSMs <= 0) b->numSMs = 1;
     cudaEventCreateWithFlags(&b->frameDone, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&b->evIn, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&b->evOut, cudaEventDisableTiming);
+    cudaStreamCreateWithFlags(&b->gstream, cudaStreamNonBlocking);
     *out = b;
     return VR_OK;
 }
@@ -1858,6 +1872,9 @@ void vr_batch_destroy(vr_batch* b) {
     cudaFree(b->dData);
     cudaFreeHost(b->hStage);
     if (b->frameDone) cudaEventDestroy(b->frameDone);
+    if (b->evIn) cudaEventDestroy(b->evIn);
+    if (b->evOut) cudaEventDestroy(b->evOut);
+    if (b->gstream) cudaStreamDestroy(b->gstream);
     delete b;
 }
 

@@ -349,7 +349,7 @@ __device__ inline f3 tempToColor(float temp) {
     const f3 b = mk3(c_scene.blackbody[i1][0], c_scene.blackbody[i1][1], c_scene.blackbody[i1][2]);
     return c_scene.leScale * (a + (b - a) * f);
 }
-__device__ inline f3 emissionWorld(f3 pw) {
+static __device__ __noinline__ f3 emissionWorld(f3 pw) {
     if (!c_scene.hasEmission) return mk3(0.f);
     return tempToColor(temperatureWorld(pw));
 }
@@ -458,6 +458,10 @@ static __device__ __noinline__ void trackVolume(const Ray& rWorld, int mip, vr::
             if (lev == 1) {
                 nodeid[0] = child;
                 t = dda.t.x - eps;
+                // the next occupied brick starts beyond the ray's end: nothing left to track
+                // (entering it would integrate over a negative interval, see the oracle's
+                // VolumeTrackingGVDB)
+                if (t >= tFar) break;
                 f3 vmin_leaf = nodeVmin(s, 0, child);
                 float4 bb = __ldg(&s.bounds[child]);
                 float bnd[3] = {bb.x * c_scene.dscale, bb.y * c_scene.dscale, bb.z * c_scene.dscale};

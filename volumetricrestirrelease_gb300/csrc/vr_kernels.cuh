@@ -92,8 +92,11 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
                 f3 albedo = sigma_s / sigma_t;
                 out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
                 float lightPdf = 0.f;
+                // Le and the emission ratio only where the medium emits: without emission the
+                // ratio luminance(0) / (0 + luminance(albedo * Ld)) is 0 or NaN -> 0, i.e. 0
+                const bool emitting = c_scene.hasEmission && density > 0.f;
                 f3 Le = mk3(0.f);
-                if (c_scene.hasEmission && density > 0.f) Le = emissionWorld(mi.p);
+                if (emitting) Le = emissionWorld(mi.p);
                 f3 oma = mk3(1.f) - albedo;
                 f3 Ld = sampleDirectLighting(sg, lightPdf, mi, o, o.lightSamples != 0, out.lightID, out.uv0, out.uv1);
                 f3 wo = -ray.d, wi = mk3(0.f);
@@ -103,8 +106,11 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
                 }
                 float p_src = out.p_y;
                 {
-                    float er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
-                    if (vr::isnan_(er)) er = 0.f;
+                    float er = 0.f;
+                    if (emitting) {
+                        er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
+                        if (vr::isnan_(er)) er = 0.f;
+                    }
                     if (vr::next1D(sg) < er) { p_src *= er; out.lightID = kSelfEmissionLightID; }
                     else p_src *= lightPdf * (1 - er);
                 }
@@ -381,7 +387,7 @@ __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBu
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const FrameParams P, const FrameBuffers B) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -505,7 +511,7 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
     }
 }
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const FrameParams P, const FrameBuffers B, const SpatialParams S) {
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -521,7 +527,7 @@ __device__ __forceinline__ void finalPixel(const FrameParams& P, const FrameBuff
     finalShade<MB>(P, B, B.cur, r, px, py);
 }
 template <int MB>
-__global__ void __launch_bounds__(128) k_final(const FrameParams P, const FrameBuffers B, int writeHist) {
+__global__ void __launch_bounds__(128) k_final(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, int writeHist) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;

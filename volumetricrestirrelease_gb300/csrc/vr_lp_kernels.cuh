@@ -97,8 +97,9 @@ static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray r
                 f3 albedo = sigma_s / sigma_t;
                 out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
                 float lightPdf = 0.f;
+                const bool emitting = c_scene.hasEmission && density > 0.f;
                 f3 Le = mk3(0.f);
-                if (c_scene.hasEmission && density > 0.f) Le = emissionWorld(mi.p);
+                if (emitting) Le = emissionWorld(mi.p);
                 f3 oma = mk3(1.f) - albedo;
                 LightSample ls;
                 const bool lv = sampleLights(mi.p, o.useEnvironmentLights != 0, o.useAnalyticLights != 0, sg, ls, out.lightID, out.uv0, out.uv1);
@@ -115,8 +116,11 @@ static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray r
                 }
                 float p_src = out.p_y;
                 {
-                    float er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
-                    if (vr::isnan_(er)) er = 0.f;
+                    float er = 0.f;      // 0 without emission (see initialSample)
+                    if (emitting) {
+                        er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
+                        if (vr::isnan_(er)) er = 0.f;
+                    }
                     if (vr::next1D(sg) < er) { p_src *= er; out.lightID = kSelfEmissionLightID; }
                     else p_src *= lightPdf * (1 - er);
                 }
@@ -203,7 +207,7 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
     (void)H;
 }
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -267,7 +271,7 @@ __device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameB
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const FrameParams P, const FrameBuffers B, const LpBuffers L) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -305,7 +309,7 @@ __device__ __forceinline__ void lpTrainSample(const FrameParams& P, const LpBuff
     L.train[2 * (size_t)i + 1] = b;
 }
 template <int MB>
-__global__ void __launch_bounds__(128) k_lp_train_gen(const FrameParams P, const LpBuffers L, uint32_t seed) {
+__global__ void __launch_bounds__(128) k_lp_train_gen(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, uint32_t seed) {
     const int i = blockIdx.x * 128 + threadIdx.x;
     if (i >= L.trainCount) return;
     lpTrainSample<MB>(P, L, seed, i);

@@ -14,6 +14,11 @@ stand in for them with the shapes, sizes and value ranges of the benchmark confi
            max path length 3, 32 candidates, temporal + 3 spatial neighbours; the camera
            orbits 0.5 deg per frame.
   small_fp16 : `small` with FP16 bricks.
+  batch  : 32 independent instances: resolutions drawn from {256^2, 512^2, 960x540, 1280x720,
+           1920x1080}, sparse fBm grids of 128^3..512^3 (seeded per instance), 8 of them fire
+           plumes (temperature 500..3000 K, blackbody emission, density falling off with
+           height); max path length 3, 16..32 candidates, temporal + spatial, FP16 bricks and
+           the learned target (2^15 training samples per instance and frame, 2^20 per batch).
   fire   : 128^3 fire plume (fBm turbulence, density falling off with height) with a
            temperature grid of 500..3000 K emitting blackbody radiance; sigma_t 30, albedo 0.6;
            one point light + dim sky; max path length 3, 16 candidates, temporal + spatial.
@@ -43,9 +48,10 @@ class SceneDesc:
     fov_deg: float = 45.0
     frames: int = 16
     fire: tuple = None             # (t_min, t_max, le_scale, cutoff, scale) for emissive plumes
+    orbit_start_deg: float = 0.0
 
     def camera(self, frame=0):
-        ang = math.radians(self.orbit_deg_per_frame * frame)
+        ang = math.radians(self.orbit_start_deg + self.orbit_deg_per_frame * frame)
         pos = (-self.camera_radius * math.sin(ang), self.camera_height, -self.camera_radius * math.cos(ang))
         c = capi.Camera()
         c.pos[:] = [float(np.float32(v)) for v in pos]
@@ -163,6 +169,38 @@ def fire(width=256, height=256, fp16=False, res=128, seed=11):
         camera_radius=2.2, frames=16, fire=(500.0, 3000.0, 100.0, 0.0, 1.0))
 
 
+BATCH_RESOLUTIONS = ((256, 256), (512, 512), (960, 540), (1280, 720), (1920, 1080))
+BATCH_GRIDS = (128, 192, 256, 320, 384, 448, 512)
+
+
+def batch(n=32, fires=8, seed=2024, learned=True, fp16=True, scale=1.0):
+    """The batched workload: a list of SceneDesc, fire plumes first.  `scale` shrinks the
+    resolutions (for tests)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        w, h = BATCH_RESOLUTIONS[int(rng.integers(len(BATCH_RESOLUTIONS)))]
+        w, h = max(8, int(w * scale)), max(8, int(h * scale))
+        M = int(rng.integers(16, 33))
+        ang = float(rng.uniform(0.0, 360.0))
+        if i < fires:
+            res = int(rng.choice((128, 192, 256)))
+            sc = fire(width=w, height=h, fp16=fp16, res=res, seed=1000 + i)
+        else:
+            res = int(rng.choice(BATCH_GRIDS))
+            sc = full(width=w, height=h, fp16=fp16)
+            sc.volume = _procedural(1, res, 6, 100 + i, float(rng.uniform(0.3, 0.4)), (-1.0, -1.0, -1.0), 2.0 / res,
+                                    fp16=fp16, num_mips=4 if res % 64 == 0 else 3, base_frequency=float(rng.uniform(2.5, 3.5)))
+        sc.name = f"batch{i}"
+        sc.options = dict(sc.options, mMaxBounces=3, mInitialM=M, mEnableTemporalReuse=1, mEnableSpatialReuse=1)
+        if learned:
+            sc.options.update(mUseLearnedPHat=1, mLearnedTrainSamples=32768, mLearnedBatch=16384)
+        sc.orbit_deg_per_frame = 0.5
+        sc.orbit_start_deg = ang
+        out.append(sc)
+    return out
+
+
 def make_volumes(sc, lib=None):
     """(density volume, temperature volume or None) of a scene."""
     from .restir import Volume
@@ -171,4 +209,4 @@ def make_volumes(sc, lib=None):
     return Volume.procedural(sc.volume, lib=lib), None
 
 
-CONFIGS = {"small": small, "full": full, "small_fp16": lambda **k: small(fp16=True, **k), "fire": fire}
+CONFIGS = {"small": small, "full": full, "small_fp16": lambda **k: small(fp16=True, **k), "fire": fire, "batch": batch}
