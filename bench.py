@@ -179,21 +179,30 @@ def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=10
     del rd
     out = torch.empty((QH, QW, 4), device="cuda")
     res = {}
+    plain_imgs = {}
+    vs_fp32 = None
     for name, (fp16, learned, M) in forms.items():
         scf = _scene(args, fp16=fp16, static=True, width=QW, height=QH)
         rd = VolumetricReSTIR(QW, QH, _options(lib, scf, learned, M).as_dict(), lib=lib)
         rd.setScene(vols[fp16], scf.medium, scf.lights, scf.env_rgb, scf.env_scale)
-        errs = []
+        errs, cross = [], []
         for f in range(frames):
             rd.execute(scf.camera(f), out.data_ptr())
             if f >= first:
                 torch.cuda.synchronize()
-                errs.append(_relmse(out.cpu().numpy(), ref))
+                img = out.cpu().numpy()
+                errs.append(_relmse(img, ref))
+                if name == "plain":
+                    plain_imgs[f] = img[..., :3].astype(np.float64)
+                elif name == "plain_fp16" and f in plain_imgs:
+                    cross.append(_relmse(img, plain_imgs[f]))
+        if cross:
+            vs_fp32 = float(np.mean(cross))
         e = np.asarray(errs)
         bm = e[: len(e) // block * block].reshape(-1, block).mean(1)
         res[name] = (float(e.mean()), float(bm.std(ddof=1) / np.sqrt(len(bm))))
         del rd
-    return res, {"resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
+    return res, {"fp16_vs_fp32_relmse": vs_fp32, "resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
                  "reference": f"{spp} spp FP64 path tracer on the GPU", "relmse": "mean over pixels and RGB of (x-r)^2/(r^2+0.01)",
                  "standard_error": f"from the means of blocks of {block} frames"}
 
@@ -402,7 +411,7 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     # ---- relMSE matching (480x270, static camera, FP64 reference) ----
-    forms = {"plain": (False, False, 32)}
+    forms = {"plain": (False, False, 32), "plain_fp16": (True, False, 32)}
     for M in LEARNED_M:
         forms[f"learned_M{M}"] = (True, True, M)
     rel, qinfo = quality(lib, vols, args, forms) if not args.no_quality else ({}, {})

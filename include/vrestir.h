@@ -283,6 +283,10 @@ int vr_render_frame_host(vr_context* ctx, const vr_camera* cam, float* out_rgba_
 int vr_render_frame_noalloc(vr_context* ctx, const vr_camera* cam, int32_t frame_index,
                             float* out_rgba_device, void* stream);
 
+/* Block size of the per-pixel kernels: 32, 64 or 128 threads (8 x 4, 8 x 8 or 8 x 16 pixels).
+ * Results do not depend on it. */
+int vr_set_block_size(vr_context* ctx, int32_t threads);
+
 /* ---- batches (no counterpart in the reference) ----
  * Many contexts -- each with its own volume, view, resolution, options, network and buffers --
  * rendered together: every pass is one persistent launch over a single list of pixel tiles of

@@ -191,3 +191,46 @@ def test_learned_options_validation(vlib, cuda):
     opts.mEnableSpatialReuse = 0
     with pytest.raises(Exception):
         VolumetricReSTIR(32, 32, opts.as_dict(), lib=vlib)
+
+
+def test_trained_network_lowers_relmse(vlib, cuda):
+    """What the trained network gains over the method without it: relMSE against an FP64
+    path-traced reference of the learned-target form with online training, against the same form
+    with a network frozen at T = 1 (zero weights: the initial RIS target without any light
+    visibility), on the small scene at a static camera."""
+    from volumetricrestirrelease_gb300 import capi, scenes
+    from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
+    W, H, frames, first = 96, 96, 48, 16
+    sc = scenes.small(width=W, height=H)
+    vol = Volume.procedural(sc.volume, lib=vlib)
+
+    def ctx(train):
+        o = capi.default_options(vlib)
+        for k, v in {**sc.options, "mUseLearnedPHat": 1, "mLearnedTrainSamples": 65536 if train else 0,
+                     "mLearnedBatch": 16384}.items():
+            setattr(o, k, v)
+        r = VolumetricReSTIR(W, H, o.as_dict(), lib=vlib)
+        r.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        if not train:
+            r.set_net_params(np.zeros(NP, np.float32))
+        return r
+
+    ref_ctx = ctx(True)
+    acc = cuda.zeros((H, W, 3), device="cuda", dtype=cuda.float64)
+    for f0 in range(0, 512, 64):
+        ref_ctx.render_reference(sc.camera(0), acc.data_ptr(), f0, 64)
+    cuda.cuda.synchronize()
+    ref = (acc / 512).cpu().numpy()
+    out = cuda.empty((H, W, 4), device="cuda", dtype=cuda.float32)
+    rel = {}
+    for name, train in (("trained", True), ("without", False)):
+        r = ctx(train)
+        errs = []
+        for f in range(frames):
+            r.execute(sc.camera(0), out.data_ptr())
+            if f >= first:
+                cuda.cuda.synchronize()
+                x = out.cpu().numpy()[..., :3].astype(np.float64)
+                errs.append(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+        rel[name] = float(np.mean(errs))
+    assert rel["trained"] < rel["without"], rel

@@ -131,6 +131,7 @@ SIGNATURES = {
     "vr_selftest_math": (_i32, [_i32, C.POINTER(_f32), C.POINTER(_f32), C.POINTER(_f32), _i32]),
     "vr_selftest_rng": (_i32, [C.POINTER(_u32), _i32, _i32, C.POINTER(_f32)]),
     "vr_selftest_umma": (_i32, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(_f32), _i32]),
+    "vr_set_block_size": (_i32, [_P, _i32]),
     "vr_batch_create": (_i32, [C.POINTER(_P), _i32, C.POINTER(_P)]),
     "vr_batch_destroy": (None, [_P]),
     "vr_batch_last_error": (C.c_char_p, [_P]),

@@ -241,6 +241,7 @@ struct vr_context {
     int launches = 0;
     int64_t h2d = 0, d2h = 0;
     int* status = nullptr;    // device status word
+    int blockThreads = 128;   // pixel kernels: blocks of 8 x (blockThreads / 8) pixels
     // learned target: network (FP32 master weights, Adam moments, BF16 copy) and the buffers
     // of the split initial pass
     float *netW = nullptr, *netM = nullptr, *netV = nullptr, *netG = nullptr, *netBias = nullptr;
@@ -1283,7 +1284,8 @@ static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStre
 template <int MB>
 static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::FrameBuffers& B, cudaStream_t st) {
     const vr_options& o = c->opts;
-    dim3 grid((c->W + 7) / 8, (c->H + 15) / 16), block(128);
+    const int rows = c->blockThreads / 8;
+    dim3 grid((c->W + 7) / 8, (c->H + rows - 1) / rows), block(c->blockThreads);
     std::vector<cudaEvent_t> frameEv;
     auto mark = [&]() {
         if (c->nev < 10) cudaEventRecord(c->ev[c->nev++], st);
@@ -1837,6 +1839,12 @@ static int batch_frame(vr_batch* b, const vr_camera* cams, float* const* outs, c
 }
 
 extern "C" {
+
+int vr_set_block_size(vr_context* c, int32_t threads) {
+    if (!c || (threads != 32 && threads != 64 && threads != 128)) return VR_ERR_INVALID_ARG;
+    c->blockThreads = threads;
+    return VR_OK;
+}
 
 int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
     if (!ctxs || !out || n < 1 || n > 1024) return VR_ERR_INVALID_ARG;

@@ -94,11 +94,35 @@ using lpn::kHid;
 using lpn::kInPad;
 using vrd::NetView;
 
+// two floats -> packed BF16 pair (lo in the low half), round to nearest even in one instruction
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+__device__ __forceinline__ float bfround(float f) { return __uint_as_float(bf16x2(f, 0.f) << 16); }
+
+// the query's 64 input features; band 0 from the hardware sine/cosine (the higher bands follow by
+// the double-angle recurrences as in lpn::encode)
 __device__ __forceinline__ void load_query(const float4* q, size_t i, float f[kInPad], const NetView& net) {
     const float4 a = q[2 * i], b = q[2 * i + 1];
     float x[3] = {a.x, a.y, a.z}, w[3] = {a.w, b.x, b.y}, s[5];
     lpn::query_scalars(x, w, net.bmin, net.binv, s);
-    lpn::encode(s, f);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        float sn, cs;
+        __sincosf(s[k] * 3.14159265358979323846f, &sn, &cs);
+#pragma unroll
+        for (int band = 0; band < lpn::kBands; ++band) {
+            f[12 * k + 2 * band] = sn;
+            f[12 * k + 2 * band + 1] = cs;
+            const float s2 = 2.f * sn * cs, c2 = cs * cs - sn * sn;
+            sn = s2;
+            cs = c2;
+        }
+    }
+#pragma unroll
+    for (int k = lpn::kIn; k < kInPad; ++k) f[k] = 0.f;
 }
 
 // Inference: persistent CTAs of 128 threads, one query per thread and tile of 128 queries.
@@ -152,10 +176,10 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 uint4 v;
-                v.x = (uint32_t)lpn::f2bf(f[8 * c + 0]) | ((uint32_t)lpn::f2bf(f[8 * c + 1]) << 16);
-                v.y = (uint32_t)lpn::f2bf(f[8 * c + 2]) | ((uint32_t)lpn::f2bf(f[8 * c + 3]) << 16);
-                v.z = (uint32_t)lpn::f2bf(f[8 * c + 4]) | ((uint32_t)lpn::f2bf(f[8 * c + 5]) << 16);
-                v.w = (uint32_t)lpn::f2bf(f[8 * c + 6]) | ((uint32_t)lpn::f2bf(f[8 * c + 7]) << 16);
+                v.x = bf16x2(f[8 * c + 0], f[8 * c + 1]);
+                v.y = bf16x2(f[8 * c + 2], f[8 * c + 3]);
+                v.z = bf16x2(f[8 * c + 4], f[8 * c + 5]);
+                v.w = bf16x2(f[8 * c + 6], f[8 * c + 7]);
                 *(uint4*)((unsigned char*)sH + umma::canon_offset(tid, 8 * c, 64)) = v;
             }
         }
@@ -185,17 +209,17 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
             if (l < 3) {
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
-                    uint32_t hb[8];
+                    float hf[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         float a = z[8 * c + j] + sBias[l * 64 + 8 * c + j];
-                        hb[j] = lpn::f2bf(a > 0.f ? a : 0.f);
+                        hf[j] = a > 0.f ? a : 0.f;
                     }
                     uint4 v;
-                    v.x = hb[0] | (hb[1] << 16);
-                    v.y = hb[2] | (hb[3] << 16);
-                    v.z = hb[4] | (hb[5] << 16);
-                    v.w = hb[6] | (hb[7] << 16);
+                    v.x = bf16x2(hf[0], hf[1]);
+                    v.y = bf16x2(hf[2], hf[3]);
+                    v.z = bf16x2(hf[4], hf[5]);
+                    v.w = bf16x2(hf[6], hf[7]);
                     *(uint4*)((unsigned char*)sH + umma::canon_offset(tid, 8 * c, 64)) = v;
                 }
             } else {
@@ -203,7 +227,7 @@ __global__ void __launch_bounds__(128) k_net_infer(NetView net, const float4* __
 #pragma unroll
                 for (int j = 0; j < kHid; ++j) {
                     float a = z[j] + sBias[192 + j];
-                    acc += lpn::round_bf(a > 0.f ? a : 0.f) * sW4[j];
+                    acc += bfround(a > 0.f ? a : 0.f) * sW4[j];
                 }
                 o = acc + *sB4;
             }
@@ -243,10 +267,10 @@ __device__ __forceinline__ void st_row_bf16(unsigned char* base, int row, const 
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         uint4 u;
-        u.x = (uint32_t)lpn::f2bf(v[8 * c + 0]) | ((uint32_t)lpn::f2bf(v[8 * c + 1]) << 16);
-        u.y = (uint32_t)lpn::f2bf(v[8 * c + 2]) | ((uint32_t)lpn::f2bf(v[8 * c + 3]) << 16);
-        u.z = (uint32_t)lpn::f2bf(v[8 * c + 4]) | ((uint32_t)lpn::f2bf(v[8 * c + 5]) << 16);
-        u.w = (uint32_t)lpn::f2bf(v[8 * c + 6]) | ((uint32_t)lpn::f2bf(v[8 * c + 7]) << 16);
+        u.x = bf16x2(v[8 * c + 0], v[8 * c + 1]);
+        u.y = bf16x2(v[8 * c + 2], v[8 * c + 3]);
+        u.z = bf16x2(v[8 * c + 4], v[8 * c + 5]);
+        u.w = bf16x2(v[8 * c + 6], v[8 * c + 7]);
         *(uint4*)(base + umma::canon_offset(row, 8 * c, K)) = u;
     }
 }
@@ -333,7 +357,7 @@ __global__ void __launch_bounds__(128, 1) k_net_train(NetView net, const float4*
 #pragma unroll
         for (int k = 0; k < 64; ++k) {
             const float a = h[k] + sBias[l * 64 + k];
-            h[k] = lpn::round_bf(a > 0.f ? a : 0.f);
+            h[k] = bfround(a > 0.f ? a : 0.f);
         }
         if (l < 3) {
             st_row_bf16(smem + ts::X, tid, h, 64);

@@ -389,7 +389,7 @@ __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBu
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     initialPixel<MB>(P, B, px, py);
 }
@@ -513,7 +513,7 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     spatialPixel<MB>(P, B, S, px, py);
 }
@@ -529,7 +529,7 @@ __device__ __forceinline__ void finalPixel(const FrameParams& P, const FrameBuff
 template <int MB>
 __global__ void __launch_bounds__(128) k_final(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, int writeHist) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     finalPixel<MB>(P, B, writeHist, px, py);
 }
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(128) k_final(const __grid_constant__ FramePara
 template <int MB>
 __global__ void __launch_bounds__(128) k_reference(const FrameParams P, int first, int count, double* accum) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     const int pid = py * P.W + px;
     const Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, P.W, P.H)), 0.f, kRayTMax};

@@ -209,7 +209,7 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     lpGeneratePixel<MB>(P, B, L, px, py);
 }
@@ -273,7 +273,7 @@ __device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameB
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
-    const int py = blockIdx.y * 16 + (threadIdx.x >> 3);
+    const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
     lpSelectPixel<MB>(P, B, L, px, py);
 }
