@@ -5,7 +5,8 @@ Bars:
     against the oracle's restatement with the same BF16 operands, within the tolerance that the
     tensor core's accumulation order leaves (relative L2 error 2e-3); the Adam update bit-exact
     given the kernel's own gradient;
-  * inference (tcgen05): T within relative 2e-3 on 99.9 % of the queries;
+  * inference (tcgen05, hardware sine/cosine for the encoding): T within relative 5e-3 on 99.9 % of
+    the queries (a BF16 rounding of a feature or an activation may land on the other side);
   * the split initial pass (generate / infer / select): training samples and the query list
     bit-exact, and -- given the GPU's T -- images, reservoirs and features bit-exact.
 """
@@ -132,7 +133,7 @@ def test_net_inference_tensor_cores(vlib, cuda):
     ref = net_forward(p, box, 1e-6, q)
     assert np.all(np.isfinite(t)) and t.std() > 0.01
     rel = np.abs(t - ref) / np.maximum(ref, 1e-6)
-    assert np.quantile(rel, 0.999) < 2e-3, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
+    assert np.quantile(rel, 0.999) < 5e-3, np.quantile(rel, [0.5, 0.99, 0.999, 1.0])
     assert rel.max() < 5e-2
 
 
@@ -168,7 +169,7 @@ def test_learned_frames_match_oracle(vlib, cuda):
         # tensor-core T of the frame against the CPU network with the same weights
         tcpu = net_forward(params, box, opts.mLearnedTFloor, qg)
         rel = np.abs(T[slots] - tcpu) / tcpu
-        assert np.quantile(rel, 0.999) < 2e-3
+        assert np.quantile(rel, 0.999) < 5e-3
         # given the GPU's T, the frame is bit-exact
         nbad = int((img.view(np.uint32) != ref.view(np.uint32)).any(-1).sum())
         assert nbad == 0, f"frame {f}: {nbad} pixels differ"
