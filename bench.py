@@ -388,6 +388,71 @@ def run_batched(args, lib):
     return res
 
 
+def run_small_configs(args, lib):
+    """The 256^2 configurations: cfg1 (plain, FP32), cfg3 (FP16 bricks), cfg4 (learned target),
+    16 frames at the static camera of the small scene; relMSE of every frame against a 4096-spp
+    FP64 reference, FP16 against FP32 frame by frame, frames/s, and the oracle on all host cores
+    for cfg1."""
+    import torch
+    from oracle import oracle as O
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
+    W = H = 256
+    sc32, sc16 = scenes.small(width=W, height=H), scenes.small(width=W, height=H, fp16=True)
+    vol32, vol16 = Volume.procedural(sc32.volume, lib=lib), Volume.procedural(sc16.volume, lib=lib)
+
+    def ctx(sc, vol, learned=False):
+        o = _options(lib, sc, learned)
+        r = VolumetricReSTIR(W, H, o.as_dict(), lib=lib)
+        r.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        return r, o
+    r, o = ctx(sc32, vol32)
+    acc = torch.zeros((H, W, 3), device="cuda", dtype=torch.float64)
+    for f0 in range(0, 4096, 256):
+        r.render_reference(sc32.camera(0), acc.data_ptr(), f0, 256)
+    torch.cuda.synchronize()
+    ref = (acc / 4096).cpu().numpy()
+    del r
+    out = torch.empty((H, W, 4), device="cuda")
+    res, imgs32 = {}, {}
+    for name, sc, vol, learned in (("cfg1_plain_fp32", sc32, vol32, False), ("cfg3_plain_fp16", sc16, vol16, False),
+                                   ("cfg4_learned_fp32", sc32, vol32, True)):
+        r, o = ctx(sc, vol, learned)
+        errs, cross = [], []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for f in range(16):
+            r.execute(sc.camera(f), out.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 16
+        r2, _ = ctx(sc, vol, learned)                  # the same 16 frames again, read back one by one
+        for f in range(16):
+            r2.execute(sc.camera(f), out.data_ptr())
+            torch.cuda.synchronize()
+            img = out.cpu().numpy()
+            errs.append(_relmse(img, ref))
+            if name == "cfg1_plain_fp32":
+                imgs32[f] = img[..., :3].astype(np.float64)
+            elif name == "cfg3_plain_fp16":
+                cross.append(_relmse(img, imgs32[f]))
+        res[name] = {"frames_per_s": 1000.0 / ms, "relmse_per_frame": errs, "relmse_frames_8_15": float(np.mean(errs[8:]))}
+        if cross:
+            res[name]["relmse_vs_fp32_per_frame"] = cross
+        del r, r2
+    # the oracle on the host cores, cfg1, all 16 frames
+    threads = os.cpu_count() or 1
+    ora = O.Oracle(W, H, _options(lib, sc32), threads=threads)
+    ora.set_volume(vol32, sc32.medium)
+    ora.set_lights(sc32.lights, sc32.env_rgb, sc32.env_scale)
+    t = time.perf_counter()
+    for f in range(16):
+        ora.render_frame(sc32.camera(f))
+    res["cfg1_cpu_oracle"] = {"frames_per_s": 16 / (time.perf_counter() - t), "cores": threads}
+    res["reference"] = "4096 spp FP64 path tracer on the GPU, static camera"
+    return res
+
+
 def run_gpu(args):
     import torch
     ws, rank = _dist()
@@ -479,6 +544,9 @@ def run_gpu(args):
     batched = None
     if not args.no_batched and rank == 0:
         batched = run_batched(args, lib)
+    small = None
+    if not args.no_small and rank == 0:
+        small = run_small_configs(args, lib)
 
     if rank != 0:
         return
@@ -531,6 +599,7 @@ def run_gpu(args):
             "roofline_tensor": roof_tc,
             "cpu_baseline": cpu,
             "batched": batched,
+            "small_configs": small,
             "clocks": clocks}
     print(json.dumps(line), flush=True)
 
@@ -546,6 +615,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-quality", action="store_true", help="skip the relMSE matching (learned form at M=32)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 32-instance form")
+    ap.add_argument("--no-small", action="store_true", help="skip the 256^2 configurations (cfg1, cfg3, cfg4)")
     ap.add_argument("--batch-steps", type=int, default=4)
     ap.add_argument("--batch-trials", type=int, default=6)
     args = ap.parse_args()
