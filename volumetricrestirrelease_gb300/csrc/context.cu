@@ -242,6 +242,10 @@ struct vr_context {
     int64_t h2d = 0, d2h = 0;
     int* status = nullptr;    // device status word
     int blockThreads = 128;   // pixel kernels: blocks of 8 x (blockThreads / 8) pixels
+    // the network trains on a side stream (non-blocking, so it also overlaps work on the legacy
+    // default stream), forked after select and joined at the end of the frame
+    cudaStream_t side = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     // learned target: network (FP32 master weights, Adam moments, BF16 copy) and the buffers
     // of the split initial pass
     float *netW = nullptr, *netM = nullptr, *netV = nullptr, *netG = nullptr, *netBias = nullptr;
@@ -494,6 +498,12 @@ __global__ void k_gather_queries(const float4* __restrict__ q, const int* __rest
 }
 #endif
 static void lp_train_steps(vr_context* c, const float4* samples, int S, cudaStream_t st, const float* ccTable = nullptr);
+static cudaEvent_t take_event(vr_context* c) {
+    cudaEvent_t e;
+    if (!c->freeEv.empty()) { e = c->freeEv.back(); c->freeEv.pop_back(); }
+    else cudaEventCreate(&e);
+    return e;
+}
 
 extern "C" {
 
@@ -641,6 +651,9 @@ void vr_destroy(vr_context* c) {
     for (auto& v : c->pendingEv) for (auto e : v) cudaEventDestroy(e);
     for (auto e : c->freeEv) cudaEventDestroy(e);
     cudaFree(c->status);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->evFork) cudaEventDestroy(c->evFork);
+    if (c->evJoin) cudaEventDestroy(c->evJoin);
     delete c;
 }
 
@@ -1078,15 +1091,15 @@ int32_t vr_last_launch_count(const vr_context* c) { return c ? c->launches : 0; 
 
 // frame events, plain: start, after the initial stage, after the spatial/final stage, end;
 // learned target: start, after generate, after infer, after select, after the spatial/final
-// stage, after the training.  Totals: 0 initial stage, 1 spatial/final stage, 2 training,
-// 3 generate, 4 infer, 5 select
+// stage, then the start and end of the training on the side stream.  Totals: 0 initial stage,
+// 1 spatial/final stage, 2 training, 3 generate, 4 infer, 5 select
 static void drain_events(vr_context* c) {
     for (auto& v : c->pendingEv) {
-        cudaEventSynchronize(v.back());
+        for (cudaEvent_t e : v) cudaEventSynchronize(e);
         static const int plain[3][3] = {{0, 1, 0}, {1, 2, 1}, {2, 3, 2}};
-        static const int learned[6][3] = {{0, 3, 0}, {3, 4, 1}, {4, 5, 2}, {0, 1, 3}, {1, 2, 4}, {2, 3, 5}};
-        const int (*map)[3] = v.size() == 6 ? learned : plain;
-        const int nm = v.size() == 6 ? 6 : (v.size() == 4 ? 3 : 0);
+        static const int learned[6][3] = {{0, 3, 0}, {3, 4, 1}, {5, 6, 2}, {0, 1, 3}, {1, 2, 4}, {2, 3, 5}};
+        const int (*map)[3] = v.size() == 7 ? learned : plain;
+        const int nm = v.size() == 7 ? 6 : (v.size() == 4 ? 3 : 0);
         for (int i = 0; i < nm; ++i) {
             float t = 0.f;
             cudaEventElapsedTime(&t, v[map[i][0]], v[map[i][1]]);
@@ -1302,6 +1315,7 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         cudaEventRecord(e, st);
         frameEv.push_back(e);
     };
+    cudaEvent_t trainEv[2] = {nullptr, nullptr};
     mark();
     const bool lpOn = lp_active(c);
     if (lpOn) {
@@ -1313,6 +1327,28 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         launch_lp_select<MB>(P, B, c->lp, grid, block, st);
         c->launches += 3;
         c->lpFrameDone = true;
+        // online training of the network on this frame's own queries (used from the next frame
+        // on), on the side stream, concurrent with the spatial pass
+        if (o.mLearnedTrainSamples > 0) {
+            if (!c->side) {
+                cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+                cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming);
+                cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming);
+            }
+            cudaEventRecord(c->evFork, st);
+            cudaStreamWaitEvent(c->side, c->evFork, 0);
+            trainEv[0] = take_event(c);
+            cudaEventRecord(trainEv[0], c->side);
+            c->lp.targetMethod = o.mLearnedTargetMethod;
+            launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(o.mLearnedSeed, c->frameCount), c->side);
+            c->launches++;
+            lp_train_steps(c, c->lp.train, o.mLearnedTrainSamples, c->side);
+            trainEv[1] = take_event(c);
+            cudaEventRecord(trainEv[1], c->side);
+            cudaEventRecord(c->evJoin, c->side);
+        } else {
+            c->lastSteps = 0;
+        }
     } else {
         launch_initial<MB>(P, B, grid, block, st);
         c->launches++;
@@ -1354,17 +1390,15 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
         mark();
     }
     c->finalBuf = totalRoundId % 2;
-    // online training of the network on this frame's own queries (used from the next frame on)
     if (lpOn) {
-        if (o.mLearnedTrainSamples > 0) {
-            c->lp.targetMethod = o.mLearnedTargetMethod;
-            launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(o.mLearnedSeed, c->frameCount), st);
-            c->launches++;
-            lp_train_steps(c, c->lp.train, o.mLearnedTrainSamples, st);
+        if (trainEv[0]) {
+            cudaStreamWaitEvent(st, c->evJoin, 0);      // the next frame infers with the new weights
+            frameEv.push_back(trainEv[0]);
+            frameEv.push_back(trainEv[1]);
         } else {
-            c->lastSteps = 0;
+            rec();
+            rec();
         }
-        mark();
     } else {
         rec();
     }
