@@ -327,13 +327,15 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
 // ---------------------------------------------------------------------------------------
 // k_initial: GenerateFeatures + TraceRays (+ TemporalReuse)
 // ---------------------------------------------------------------------------------------
-// Register budget: 5 blocks of 128 threads per SM (<= 102 registers per thread).  Measured on
-// the full workload against 1, 4 and 6 blocks; the extra residency outweighs the added spills.
+// Register budget: 16 blocks of 128 threads per SM, i.e. full occupancy at 32 registers per
+// thread.  The pixel kernels are bound by dependent-load and branch latency, not by issue, so
+// residency pays for the spills: measured on the full workload against 4, 5, 6, 8, 10 and 12
+// blocks, each step up was faster (candidate generation 115 ms at 5 blocks, 93 ms at 16).
 #ifndef VR_KINIT_MIN_BLOCKS
-#define VR_KINIT_MIN_BLOCKS 5
+#define VR_KINIT_MIN_BLOCKS 16
 #endif
 #ifndef VR_KSPAT_MIN_BLOCKS
-#define VR_KSPAT_MIN_BLOCKS 5
+#define VR_KSPAT_MIN_BLOCKS 16
 #endif
 template <int MB>
 __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBuffers& B, int px, int py) {
