@@ -388,8 +388,8 @@ __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBu
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
-template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
+template <int MB, int OCC = VR_KINIT_MIN_BLOCKS>
+__global__ void __launch_bounds__(128, OCC) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -512,8 +512,8 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
         finalShade<MB>(P, B, outb, result, px, py);
     }
 }
-template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
+template <int MB, int OCC = VR_KSPAT_MIN_BLOCKS>
+__global__ void __launch_bounds__(128, OCC) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
