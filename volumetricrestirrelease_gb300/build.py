@@ -57,9 +57,6 @@ def build(force=False, jobs=None):
         obj = BUILD / f"frame_kernels_mb{mb}.o"
         src = CSRC / "frame_kernels.cu"
         units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-c", str(src), "-o", str(obj)]))
-        # the initial and spatial kernels again at 5 blocks per SM, for frames below a few waves
-        obj = BUILD / f"frame_kernels_lo_mb{mb}.o"
-        units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + [f"-DVR_MB={mb}", "-DVR_LOW_OCC=5", "-c", str(src), "-o", str(obj)]))
     for mb in (1, 2, 3, 4):
         obj = BUILD / f"batch_mb{mb}.o"
         src = CSRC / "batch.cu"

@@ -33,12 +33,7 @@ namespace vrk {
     void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);        \
     void launch_lp_generate_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
     void launch_lp_select_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
-    void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);          \
-    cudaError_t upload_scene_lo_##MB(const vrd::DevScene&, cudaStream_t);                                      \
-    void launch_initial_lo_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, dim3, dim3, cudaStream_t);  \
-    void launch_spatial_lo_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::SpatialParams&, dim3, dim3, cudaStream_t); \
-    void launch_lp_generate_lo_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
-    void launch_lp_select_lo_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t);
+    void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);
 VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 #undef VR_DECL
 // the network kernels (lp.cu)
@@ -640,8 +635,6 @@ vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int
     if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) { delete c; if (err) *err = VR_ERR_OOM; return nullptr; }
     cudaMemset(c->status, 0, sizeof(int));
     c->scene.status = c->status;
-    cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, 0);
-    if (c->numSMs <= 0) c->numSMs = 1;
     if (err) *err = VR_OK;
     return c;
 }
@@ -912,22 +905,13 @@ static int prepare_frame(vr_context* c, const vr_camera* cam) {
     return VR_OK;
 }
 
-// The initial and spatial kernels come in two register budgets: 16 blocks of 128 threads per SM
-// (full occupancy; the pixel loops are latency-bound) and 5 blocks per SM, which is faster when
-// the frame has too few blocks to keep 16 per SM busy for a couple of waves (256^2: 512 blocks).
-static bool low_occupancy(const vr_context* c) {
-    const int64_t blocks = ((int64_t)c->W * c->H + 127) / 128;
-    return blocks < (int64_t)2 * 16 * std::max(1, c->numSMs);
-}
-
 static int upload_scene(vr_context* c, cudaStream_t st) {
     cudaError_t e;
-    const bool lo = low_occupancy(c);
     switch (c->opts.mMaxBounces) {
-        case 1: e = vrk::upload_scene_1(c->scene, st); if (lo && e == cudaSuccess) e = vrk::upload_scene_lo_1(c->scene, st); break;
-        case 2: e = vrk::upload_scene_2(c->scene, st); if (lo && e == cudaSuccess) e = vrk::upload_scene_lo_2(c->scene, st); break;
-        case 3: e = vrk::upload_scene_3(c->scene, st); if (lo && e == cudaSuccess) e = vrk::upload_scene_lo_3(c->scene, st); break;
-        default: e = vrk::upload_scene_4(c->scene, st); if (lo && e == cudaSuccess) e = vrk::upload_scene_lo_4(c->scene, st); break;
+        case 1: e = vrk::upload_scene_1(c->scene, st); break;
+        case 2: e = vrk::upload_scene_2(c->scene, st); break;
+        case 3: e = vrk::upload_scene_3(c->scene, st); break;
+        default: e = vrk::upload_scene_4(c->scene, st); break;
     }
     if (e != cudaSuccess) { c->err = std::string("scene upload: ") + cudaGetErrorString(e); return VR_ERR_CUDA; }
     return VR_OK;
@@ -1244,28 +1228,14 @@ int vr_last_transfer_bytes(const vr_context* c, int64_t* h2d, int64_t* d2h) {
 // frame launch sequence (VolumetricReSTIR.cpp:499-762)
 // ---------------------------------------------------------------------------------------
 template <int MB>
-static void launch_initial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, dim3 g, dim3 b, cudaStream_t st, bool lo) {
-    if (lo) {
-        if (MB == 1) vrk::launch_initial_lo_1(P, B, g, b, st);
-        else if (MB == 2) vrk::launch_initial_lo_2(P, B, g, b, st);
-        else if (MB == 3) vrk::launch_initial_lo_3(P, B, g, b, st);
-        else vrk::launch_initial_lo_4(P, B, g, b, st);
-        return;
-    }
+static void launch_initial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, dim3 g, dim3 b, cudaStream_t st) {
     if (MB == 1) vrk::launch_initial_1(P, B, g, b, st);
     else if (MB == 2) vrk::launch_initial_2(P, B, g, b, st);
     else if (MB == 3) vrk::launch_initial_3(P, B, g, b, st);
     else vrk::launch_initial_4(P, B, g, b, st);
 }
 template <int MB>
-static void launch_spatial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st, bool lo) {
-    if (lo) {
-        if (MB == 1) vrk::launch_spatial_lo_1(P, B, S, g, b, st);
-        else if (MB == 2) vrk::launch_spatial_lo_2(P, B, S, g, b, st);
-        else if (MB == 3) vrk::launch_spatial_lo_3(P, B, S, g, b, st);
-        else vrk::launch_spatial_lo_4(P, B, S, g, b, st);
-        return;
-    }
+static void launch_spatial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st) {
     if (MB == 1) vrk::launch_spatial_1(P, B, S, g, b, st);
     else if (MB == 2) vrk::launch_spatial_2(P, B, S, g, b, st);
     else if (MB == 3) vrk::launch_spatial_3(P, B, S, g, b, st);
@@ -1280,28 +1250,14 @@ static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, 
 }
 
 template <int MB>
-static void launch_lp_generate(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st, bool lo) {
-    if (lo) {
-        if (MB == 1) vrk::launch_lp_generate_lo_1(P, B, L, g, b, st);
-        else if (MB == 2) vrk::launch_lp_generate_lo_2(P, B, L, g, b, st);
-        else if (MB == 3) vrk::launch_lp_generate_lo_3(P, B, L, g, b, st);
-        else vrk::launch_lp_generate_lo_4(P, B, L, g, b, st);
-        return;
-    }
+static void launch_lp_generate(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
     if (MB == 1) vrk::launch_lp_generate_1(P, B, L, g, b, st);
     else if (MB == 2) vrk::launch_lp_generate_2(P, B, L, g, b, st);
     else if (MB == 3) vrk::launch_lp_generate_3(P, B, L, g, b, st);
     else vrk::launch_lp_generate_4(P, B, L, g, b, st);
 }
 template <int MB>
-static void launch_lp_select(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st, bool lo) {
-    if (lo) {
-        if (MB == 1) vrk::launch_lp_select_lo_1(P, B, L, g, b, st);
-        else if (MB == 2) vrk::launch_lp_select_lo_2(P, B, L, g, b, st);
-        else if (MB == 3) vrk::launch_lp_select_lo_3(P, B, L, g, b, st);
-        else vrk::launch_lp_select_lo_4(P, B, L, g, b, st);
-        return;
-    }
+static void launch_lp_select(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
     if (MB == 1) vrk::launch_lp_select_1(P, B, L, g, b, st);
     else if (MB == 2) vrk::launch_lp_select_2(P, B, L, g, b, st);
     else if (MB == 3) vrk::launch_lp_select_3(P, B, L, g, b, st);
@@ -1343,7 +1299,6 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     const vr_options& o = c->opts;
     const int rows = c->blockThreads / 8;
     dim3 grid((c->W + 7) / 8, (c->H + rows - 1) / rows), block(c->blockThreads);
-    const bool lo = low_occupancy(c);
     std::vector<cudaEvent_t> frameEv;
     auto mark = [&]() {
         if (c->nev < 10) cudaEventRecord(c->ev[c->nev++], st);
@@ -1365,11 +1320,11 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     const bool lpOn = lp_active(c);
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
-        launch_lp_generate<MB>(P, B, c->lp, grid, block, st, lo);
+        launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
         rec();
         vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
         rec();
-        launch_lp_select<MB>(P, B, c->lp, grid, block, st, lo);
+        launch_lp_select<MB>(P, B, c->lp, grid, block, st);
         c->launches += 3;
         c->lpFrameDone = true;
         // online training of the network on this frame's own queries (used from the next frame
@@ -1395,7 +1350,7 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             c->lastSteps = 0;
         }
     } else {
-        launch_initial<MB>(P, B, grid, block, st, lo);
+        launch_initial<MB>(P, B, grid, block, st);
         c->launches++;
     }
     mark();
@@ -1424,7 +1379,7 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             S.writeHistory = temporal;
             int r2 = ((o.mSpatialReuseRounds + 1) * c->frameCount + r) % 16;
             neighbor_offsets(o, r2, S.offs);
-            launch_spatial<MB>(P, B, S, grid, block, st, lo);
+            launch_spatial<MB>(P, B, S, grid, block, st);
             c->launches++;
             totalRoundId++;
             if (S.last) mark();

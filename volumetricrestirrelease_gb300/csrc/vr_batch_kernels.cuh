@@ -26,13 +26,8 @@ __device__ __forceinline__ void blockCopy(T* dst, const T* src) {
 #endif
 }
 
-// The persistent batch kernel keeps the register budget it was validated with (5 blocks of 128
-// threads per SM, <= 102 registers); its grid is blocks_per_sm x SMs, blocks_per_sm <= 8.
-#ifndef VR_KBATCH_MIN_BLOCKS
-#define VR_KBATCH_MIN_BLOCKS 5
-#endif
 template <int MB, int PASS>
-__global__ void __launch_bounds__(128, VR_KBATCH_MIN_BLOCKS) kb_pixels(const BatchLaunch BL) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_pixels(const BatchLaunch BL) {
     __shared__ FrameParams sP;
     __shared__ FrameBuffers sB;
     __shared__ LpBuffers sL;

@@ -586,12 +586,7 @@ struct SampleDist {
     float hit[4], tr[4], pdf[4];
     int n; float thick = 0.f; float tNear, tFar; Ray ray; bool init = false; bool lin = false;
     __device__ void setRay(float a, float b, const Ray& r) { tNear = a; tFar = b; ray = r; }
-    __device__ void start() {
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (i < n) hit[i] = -1;
-        init = true;
-    }
+    __device__ void start() { for (int i = 0; i < n; i++) hit[i] = -1; init = true; }
     __device__ static float thickAt(float t, float c3, float c2, float c1, float c0) {
         float t2 = t * t, t3 = t2 * t, t4 = t2 * t2;
         return c3 * t4 / 4 + c2 * t3 / 3 + c1 * t2 / 2 + c0 * t;
@@ -659,13 +654,10 @@ struct SampleDist {
     }
     __device__ void end() {
         if (init) {
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (k < n && hit[k] == -1) { hit[k] = kRayTMax; tr[k] = vr::exp_(-thick); pdf[k] = tr[k]; }
+            for (int k = 0; k < n; k++)
+                if (hit[k] == -1) { hit[k] = kRayTMax; tr[k] = vr::exp_(-thick); pdf[k] = tr[k]; }
         } else {
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (k < n) { hit[k] = kRayTMax; tr[k] = 1.f; pdf[k] = 1.f; }
+            for (int k = 0; k < n; k++) { hit[k] = kRayTMax; tr[k] = 1.f; pdf[k] = 1.f; }
         }
     }
 };
@@ -828,11 +820,7 @@ static __device__ __noinline__ float computeVisibility(const Ray& ray, vr::Rng& 
 }
 __device__ inline void sampleDistances(const Ray& r, vr::Rng& sg, bool lin, int mip, int n, float hit[4], float pdf[4], float tr[4]) {
     SampleDist a; a.n = n; a.lin = lin;
-    if (lin) {
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (i < n) a.tr[i] = -vr::log_(1 - vr::next1D(sg));
-    }
+    if (lin) for (int i = 0; i < n; i++) a.tr[i] = -vr::log_(1 - vr::next1D(sg));
     trackVolume(r, mip, sg, a, lin);
     for (int i = 0; i < 4; ++i) { hit[i] = a.hit[i]; pdf[i] = a.pdf[i]; tr[i] = a.tr[i]; }
 }

@@ -327,15 +327,13 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
 // ---------------------------------------------------------------------------------------
 // k_initial: GenerateFeatures + TraceRays (+ TemporalReuse)
 // ---------------------------------------------------------------------------------------
-// Register budget: 16 blocks of 128 threads per SM, i.e. full occupancy at 32 registers per
-// thread.  The pixel kernels are bound by dependent-load and branch latency, not by issue, so
-// residency pays for the spills: measured on the full workload against 4, 5, 6, 8, 10 and 12
-// blocks, each step up was faster (candidate generation 115 ms at 5 blocks, 93 ms at 16).
+// Register budget: 5 blocks of 128 threads per SM (<= 102 registers per thread).  Measured on
+// the full workload against 1, 4 and 6 blocks; the extra residency outweighs the added spills.
 #ifndef VR_KINIT_MIN_BLOCKS
-#define VR_KINIT_MIN_BLOCKS 16
+#define VR_KINIT_MIN_BLOCKS 5
 #endif
 #ifndef VR_KSPAT_MIN_BLOCKS
-#define VR_KSPAT_MIN_BLOCKS 16
+#define VR_KSPAT_MIN_BLOCKS 5
 #endif
 template <int MB>
 __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBuffers& B, int px, int py) {
@@ -388,8 +386,8 @@ __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBu
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
-template <int MB, int OCC = VR_KINIT_MIN_BLOCKS>
-__global__ void __launch_bounds__(128, OCC) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_initial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -512,8 +510,8 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
         finalShade<MB>(P, B, outb, result, px, py);
     }
 }
-template <int MB, int OCC = VR_KSPAT_MIN_BLOCKS>
-__global__ void __launch_bounds__(128, OCC) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ SpatialParams S) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;

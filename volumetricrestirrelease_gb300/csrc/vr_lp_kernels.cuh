@@ -206,8 +206,8 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
     L.rng[pid] = make_uint4(sg.s[0], sg.s[1], sg.s[2], sg.s[3]);
     (void)H;
 }
-template <int MB, int OCC = VR_KINIT_MIN_BLOCKS>
-__global__ void __launch_bounds__(128, OCC) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
@@ -270,8 +270,8 @@ __device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameB
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
-template <int MB, int OCC = VR_KINIT_MIN_BLOCKS>
-__global__ void __launch_bounds__(128, OCC) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
