@@ -119,6 +119,9 @@ typedef struct vr_options {
     uint32_t mLearnedSeed;                      /* 1: weight initialisation and training streams */
     uint32_t mLearnedTargetMethod;              /* VR_TRACK_RAY_MARCHING: estimator of the training targets (mip 0) */
     int32_t mLearnedLoss;                       /* 0: squared error of T; 1: squared error of log T (targets floored) */
+    /* animated volumes (VolumetricReSTIR.h:152): evaluate the temporal tap's MIS weight on the
+     * previous animation frame's grids (VolumeDesc.usePrevGridForReproj) */
+    int32_t mUsePrevVolumeForReproj;            /* 1 */
 } vr_options;
 
 /* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */
@@ -222,6 +225,10 @@ int vr_volume_create_procedural(const vr_procedural_desc* d, vr_volume** out);
 int vr_volume_create_dense(const float* density, int32_t res, int32_t num_mips,
                            const float world_min[3], float voxel_size, int32_t fp16,
                            vr_volume** out);
+/* A signed scalar grid, mip 0 only (velocity components for vr_set_animation): bricks wherever
+ * a voxel is nonzero, values stored as given.  values: res^3, x fastest. */
+int vr_volume_create_dense_signed(const float* values, int32_t res, const float world_min[3], float voxel_size,
+                                  int32_t fp16, vr_volume** out);
 void vr_volume_destroy(vr_volume* v);
 int vr_volume_get_info(const vr_volume* v, vr_volume_info* info);
 int vr_volume_get_slot(const vr_volume* v, int32_t slot, vr_grid_view* view);
@@ -259,6 +266,28 @@ int vr_set_lights(vr_context* ctx, const vr_point_light* lights, int32_t num_lig
  * temperature NULL switches emission off.  Resets the history like an option change. */
 int vr_set_emission(vr_context* ctx, const vr_volume* temperature, float le_scale, float cutoff,
                     float scale, const float* lut_rgb);
+
+/* Animated volume sequences (Scene::addGVDBVolumeSequence, Scene.cpp:3329-3354; the per-frame
+ * advance of Scene::update, Scene.cpp:825-860; the previous-frame grids of the temporal pass,
+ * ReSTIRHelper.slang:95-96, 450-452, TemporalReuse.cs.slang:161-166).
+ *
+ * frames[0..n): the density volumes of the sequence, each with the res, mip count and voxel size
+ * of the volume given to vr_set_volume (whose medium they use), placed anywhere in the world.  temperature: NULL, or n
+ * entries (an entry may be NULL: that frame does not emit), read like vr_set_emission's grid
+ * with the parameters of the last vr_set_emission call (the reference's defaults 0.005, 1, 100
+ * and the built-in table if there was none).  velocity: NULL, or 3n scalar volumes, the x, y
+ * and z components of frame i at [3i, 3i+2], in world units per frame; the temporal
+ * reprojection moves the reprojected point back by velocity * velocity_scale.
+ *
+ * Every vr_render_frame advances the sequence by one frame, cyclically; the first rendered frame
+ * is frame 0 and the previous frame of frame 0 is frame n-1.  The frames stay resident in device
+ * memory.  With mUsePrevVolumeForReproj the temporal tap's MIS weight evaluates the current
+ * sample on the previous frame's grids.  n = 0 returns to the static volume.  Resets the history
+ * like an option change.  Not available in batches. */
+int vr_set_animation(vr_context* ctx, const vr_volume* const* frames, int32_t n, const vr_volume* const* temperature,
+                     const vr_volume* const* velocity, float velocity_scale);
+/* Index of the animation frame rendered last (-1 before the first frame or without animation). */
+int32_t vr_animation_frame(const vr_context* ctx);
 
 /* ---- per-frame call (execute, VolumetricReSTIR.cpp:303-906) ----
  * out_rgba_device: width*height float4 (RGBA32F, `accumulated_color`), device memory.

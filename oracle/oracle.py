@@ -40,6 +40,7 @@ def _load():
         "vro_splitmix": (None, [C.c_uint64, C.c_int, P]),
         "vro_set_net": (None, [P, P, P, P]),
         "vro_set_emission": (None, [P, P, P, C.c_float, C.c_float, C.c_float]),
+        "vro_set_animation": (None, [P, P, C.c_int, P, P, C.c_float, P, C.c_float, C.c_float, C.c_float]),
         "vro_set_lp_T": (None, [P, P, C.c_int64]),
         "vro_export_lp": (C.c_int64, [P, C.c_int, P, C.c_int64]),
         "vro_net_forward": (None, [P, P, P, C.c_float, P, C.c_int, P]),
@@ -116,11 +117,42 @@ class Oracle:
             raise RuntimeError(f"oracle reference status {r}")
         return accum
 
+    def set_animation(self, frames, temperature=None, velocity=None, velocity_scale=1.0):
+        """Mirror of VolumetricReSTIR.set_animation: frames (density volumes), temperature (one
+        per frame, entries may be None) and velocity (3 component volumes per frame)."""
+        from volumetricrestirrelease_gb300 import capi
+        from volumetricrestirrelease_gb300.restir import blackbody_lut
+        n = len(frames)
+        self._anim_keep = list(frames) + list(temperature or []) + list(velocity or [])
+        views = (capi.GridView * max(1, 16 * n))()
+        for i, f in enumerate(frames):
+            fv = f.views()
+            for k in range(16):
+                views[16 * i + k] = fv[k]
+        tv = vv = None
+        if temperature is not None:
+            tv = (capi.GridView * n)()
+            for i, t in enumerate(temperature):
+                if t is not None:
+                    tv[i] = t.slot(0)
+        if velocity is not None:
+            vv = (capi.GridView * (3 * n))()
+            for i, v in enumerate(velocity):
+                vv[i] = v.slot(0)
+        # the parameters of the last set_emission, else Scene::addGVDBVolume's defaults
+        le, cut, sc, lut = getattr(self, "_emis_params", (0.005, 1.0, 100.0, None))
+        self._anim_lut = np.ascontiguousarray(blackbody_lut() if lut is None else lut, np.float32).reshape(384)
+        self._anim_arrays = (views, tv, vv)
+        self.L.vro_set_animation(self._h, C.cast(views, C.c_void_p), n, C.cast(tv, C.c_void_p) if tv is not None else None,
+                                 C.cast(vv, C.c_void_p) if vv is not None else None, velocity_scale, _ptr(self._anim_lut),
+                                 le, cut, sc)
+
     def set_emission(self, temperature, le_scale, cutoff=0.0, scale=1.0, lut=None):
         from volumetricrestirrelease_gb300.restir import blackbody_lut
         if temperature is None:
             self.L.vro_set_emission(self._h, None, None, 0.0, 0.0, 1.0)
             return
+        self._emis_params = (le_scale, cutoff, scale, lut)
         self._tview = temperature.slot(0)
         self._tvol = temperature
         self._lut = np.ascontiguousarray(blackbody_lut() if lut is None else lut, np.float32).reshape(384)

@@ -179,13 +179,23 @@ struct MediumI {
 struct Emission {             // VolumeDesc.hasEmission, LeScale, temperatureCutOff/Scale + the LUT
     bool has = false;
     Slot slot;                 // temperature grid, mip 0
+    bool lastHas = false;      // VolumeDesc.lastFrameHasEmission
+    Slot prevSlot;             // the previous animation frame's temperature grid
     float leScale = 0.f, cutoff = 0.f, scale = 1.f;
     float lut[128][3];
 };
 
+// slots [kPrevSlotOffset, kPrevSlotOffset + VR_NUM_SLOTS): the previous animation frame's mips
+// (the role of kPrevFrameDensityGridOffset, HostDeviceSharedConstants.slang:27)
+constexpr int kPrevSlotOffset = VR_NUM_SLOTS;
+
 struct Scene {
-    Slot slots[VR_NUM_SLOTS];
+    Slot slots[2 * VR_NUM_SLOTS];
     MediumI med;
+    // VolumeDesc.hasAnimation / usePrevGridForReproj / hasVelocity / velocityScale
+    bool hasAnimation = false, usePrevGrid = true, hasVelocity = false;
+    float velocityScale = 1.f;
+    Slot vel[3];               // velocity components, world units per frame
     std::vector<vr_point_light> lights;
     EnvMap env;
     bool hasEnv = false;
@@ -316,8 +326,8 @@ static float DensityWorldSpace(const Scene& sc, f3 p, int mip) { return Density(
 // TemperatureWorldSpace / ConvertTempToColor / EmissionWorldSpace (VolumeBase.slang:196-232);
 // the LUT's hardware linear filter restated in software: texel centres at (i + 0.5) / 128,
 // clamped addressing
-static float TemperatureWorldSpace(const Scene& sc, f3 pw) {
-    const Slot& s = sc.emis.slot;
+static float TemperatureWorldSpace(const Scene& sc, f3 pw, bool isLastFrame = false) {
+    const Slot& s = isLastFrame ? sc.emis.prevSlot : sc.emis.slot;
     f3 p = mulPoint(pw, s.M);
     if (p.x < s.bmin[0] || p.y < s.bmin[1] || p.z < s.bmin[2] || p.x >= s.bmax[0] || p.y >= s.bmax[1] || p.z >= s.bmax[2]) return 0.f;
     f3 vmin;
@@ -338,9 +348,24 @@ static f3 ConvertTempToColor(const Scene& sc, float temp) {
     const f3 b = mk3(sc.emis.lut[i1][0], sc.emis.lut[i1][1], sc.emis.lut[i1][2]);
     return sc.emis.leScale * (a + (b - a) * f);
 }
-static f3 EmissionWorldSpace(const Scene& sc, f3 pw) {
-    if (!sc.emis.has) return mk3(0.f);
-    return ConvertTempToColor(sc, TemperatureWorldSpace(sc, pw));
+static f3 EmissionWorldSpace(const Scene& sc, f3 pw, bool isLastFrame = false) {
+    if (isLastFrame ? !sc.emis.lastHas : !sc.emis.has) return mk3(0.f);
+    return ConvertTempToColor(sc, TemperatureWorldSpace(sc, pw, isLastFrame));
+}
+// VelocityWorld (VolumeBase.slang:182-194): trilinear velocity at mip 0 of each component grid,
+// zero outside them (NaN coordinates included)
+static f3 VelocityWorld(const Scene& sc, f3 pw) {
+    float v[3];
+    for (int k = 0; k < 3; ++k) {
+        const Slot& s = sc.vel[k];
+        const f3 p = mulPoint(pw, s.M);
+        v[k] = 0.f;
+        if (!(p.x >= s.bmin[0] && p.y >= s.bmin[1] && p.z >= s.bmin[2] && p.x < s.bmax[0] && p.y < s.bmax[1] && p.z < s.bmax[2])) continue;
+        f3 vmin;
+        const int br = findBrick(s, p, vmin);
+        if (br >= 0) v[k] = trilinear(s, br, p - vmin);
+    }
+    return mk3(v[0], v[1], v[2]);
 }
 
 // Bounds3f::IntersectP + IntersectVolumeBound (VolumeBase.slang:131-172)
@@ -849,7 +874,8 @@ static float MediumTrResidualRatioTrackingGeneric(const Scene& sc, const Ray& r,
     return a.Tr;
 }
 static float MediumTrRayMarchingGeneric(const Scene& sc, const Ray& r, int mip, bool lin, float tStepScale, Rng& sg) {
-    int eff = mip >= kNumMaxMips ? mip - kNumMaxMips : mip;
+    int eff = mip >= kPrevSlotOffset ? mip - kPrevSlotOffset : mip;
+    eff = eff >= kNumMaxMips ? eff - kNumMaxMips : eff;
     MediumTrRayMarchingAdapter a(sc, lin, sc.med.tStep * tStepScale * (float)(eff + 1));
     VolumeTrackingGVDB(sc, r, mip, sg, a, false);
     return a.Tr;
@@ -1540,7 +1566,8 @@ struct ExtraProvider {        // StructuredBuffer/Array data providers (ArrayDat
     f3 get(int i) const { return data[i]; }
 };
 
-static f3 evaluate_L_in_volume(const Ctx& c, const MediumInteraction& mi, int lightID, const float lightUV[2], Rng& sg, const SamplingOptions& options, bool cullNonOpaque) {
+static f3 evaluate_L_in_volume(const Ctx& c, const MediumInteraction& mi, int lightID, const float lightUV[2], Rng& sg, const SamplingOptions& options, bool cullNonOpaque,
+                               int densityGridOffset) {
     const Scene& sc = *c.sc;
     Ray shadowRay;
     f3 Ld = mk3(0.f);
@@ -1556,15 +1583,16 @@ static f3 evaluate_L_in_volume(const Ctx& c, const MediumInteraction& mi, int li
     } else {
         return mk3(0.f);      // mesh lights are outside this path
     }
-    float Tr = computeVisibility(sc, shadowRay, sg, options.lightSamples, cullNonOpaque ? options.lightingMipLevel : 0,
+    float Tr = computeVisibility(sc, shadowRay, sg, options.lightSamples, cullNonOpaque ? options.lightingMipLevel + densityGridOffset : 0,
                                  options.lightingUseLinearSampler, options.lightingTrackingMethod, options.lightingTStepScale);
     return Tr * Ld;
 }
 
 static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, Ray ray, Rng& sg, const SamplingOptions& options,
-                      bool noReuse, bool isFinalShading) {
+                      bool noReuse, bool isFinalShading, bool isLastFrame = false) {
     const Scene& sc = *c.sc;
-    const int mipLevelOffset = 0;
+    const bool useLastFrameGrid = sc.usePrevGrid && isLastFrame && sc.hasAnimation;
+    const int mipLevelOffset = useLastFrameGrid ? kPrevSlotOffset : 0;
     bool isBackgroundSample = tap.depth == kRayTMax;
     ray.tMax = tap.depth;
     f3 F = mk3(1.f);
@@ -1590,7 +1618,7 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
         if (isBackgroundSample) {
             F = F * envEval(sc, ray.dir);
         } else if (isSelfEmission) {
-            F = F * EmissionWorldSpace(*c.sc, p_World);
+            F = F * EmissionWorldSpace(*c.sc, p_World, useLastFrameGrid);
         } else {
             bool isScatterSelfEmission = false;
             Ray scatterRay{};
@@ -1639,17 +1667,18 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                     mi.p = p_World;
                     if (all_eq0(F)) return mk3(0.f);
                 }
-                if (isScatterSelfEmission) F = F * EmissionWorldSpace(*c.sc, p_World);
+                if (isScatterSelfEmission) F = F * EmissionWorldSpace(*c.sc, p_World, useLastFrameGrid);
                 else mi = MediumInteraction{scatterRay.at(scatterRay.tMax), -scatterRay.dir, sc.med.g, true};
             }
             if (!isScatterSelfEmission && any_gt0(F))
-                F = F * evaluate_L_in_volume(c, mi, tap.lightID, tap.lightUV, sg, options, !isFinalShading);
+                F = F * evaluate_L_in_volume(c, mi, tap.lightID, tap.lightUV, sg, options, !isFinalShading, mipLevelOffset);
         }
     }
     return F;
 }
-static float evaluate_P_hat(const Ctx& c, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o, const Reservoir& tap) {
-    f3 F = evaluate_F_(c, tap, extra, ray, sg, o, false, false);
+static float evaluate_P_hat(const Ctx& c, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o, const Reservoir& tap,
+                            bool isLastFrame = false) {
+    f3 F = evaluate_F_(c, tap, extra, ray, sg, o, false, false, isLastFrame);
     return luminance(F);
 }
 static void resampleNeighbor(const Ctx& c, Reservoir& tap, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o) {
@@ -1729,6 +1758,36 @@ struct Oracle {
     std::vector<Features> features, temporalFeatures;
     std::vector<float> color;          // perPixelColor[0] (reference mode), rgba
     int lastMaxBounces = 0;
+
+    // animated volume (Scene::addGVDBVolumeSequence / Scene::update): every frame's grids, the
+    // current one advanced before each rendered frame
+    struct AnimFrame {
+        Slot slots[VR_NUM_SLOTS];
+        Slot temp, vel[3];
+        bool hasTemp = false;
+    };
+    std::vector<AnimFrame> anim;
+    Slot staticSlots[VR_NUM_SLOTS];
+    int animId = -1;
+    bool animTemp = false, animVel = false;
+    float animVelScale = 1.f;
+    void animAdvance() {
+        if (anim.empty()) return;
+        const int n = (int)anim.size();
+        animId = (animId + 1) % n;
+        const int cur = animId, prv = (cur + n - 1) % n;
+        for (int k = 0; k < VR_NUM_SLOTS; ++k) { sc.slots[k] = anim[cur].slots[k]; sc.slots[kPrevSlotOffset + k] = anim[prv].slots[k]; }
+        sc.hasAnimation = true;
+        if (animTemp) {
+            sc.emis.slot = anim[cur].temp; sc.emis.prevSlot = anim[prv].temp;
+            sc.emis.has = anim[cur].hasTemp; sc.emis.lastHas = anim[prv].hasTemp;
+        }
+        if (animVel) {
+            for (int k = 0; k < 3; ++k) sc.vel[k] = anim[cur].vel[k];
+            sc.hasVelocity = true;
+            sc.velocityScale = animVelScale;
+        }
+    }
 
     // learned target: network parameters and box, optional externally supplied T per vertex
     // slot, and the frame's per-slot queries and training samples (exports for the tests)
@@ -2090,6 +2149,12 @@ struct Oracle {
                     if (reprojDepth == kRayTMax && opts.mTemporalReprojectionMode != VR_REPROJ_NO_BACKGROUND && !isBackgroundReservoir)
                         reprojDepth = RejectionSampleRandomPointByDensity(sc, ray, sg, kNumMaxMips + opts.mTemporalReprojectionMipLevel);
                     f3 p = ray.origin + ray.dir * reprojDepth;
+                    // find last frame world position if having velocity grid (TemporalReuse.cs.slang:161-166);
+                    // a background point keeps its own pixel below and needs none
+                    if (sc.hasVelocity && sc.hasAnimation && reprojDepth != kRayTMax) {
+                        f3 v = VelocityWorld(sc, p) * sc.velocityScale;
+                        p = p - v;
+                    }
                     float in4[4] = {p.x, p.y, p.z, 1.f}, vp[4], cp[4];
                     mulMat4(prev.view, in4, vp);
                     mulMat4(prev.proj, vp, cp);
@@ -2164,7 +2229,7 @@ struct Oracle {
                                        i == 0 ? centerPrevFrameDepth : temporalOriginalDepth};
                                 float backupDepth = taps[i].depth;
                                 taps[i].depth = nr.tMax;
-                                float p_y = evaluate_P_hat(cl, nr, sg, i == 0 ? curProv : tempProv, cl.spatial, taps[i]);
+                                float p_y = evaluate_P_hat(cl, nr, sg, i == 0 ? curProv : tempProv, cl.spatial, taps[i], true);
                                 taps[i].depth = backupDepth;
                                 if (isinf_(p_y) || isnan_(p_y)) p_y = 0.f;
                                 p_sum += p_y * correctedM;
@@ -2332,6 +2397,7 @@ struct Oracle {
     // VolumetricReSTIR::execute (VolumetricReSTIR.cpp:303-906)
     void renderFrame(const vr_camera& camIn, float* outRGBA, float* mvec) {
         if (optionsChanged) { frameCount = 0; temporalSampleAccumulated = 0; optionsChanged = false; }
+        sc.usePrevGrid = opts.mUsePrevVolumeForReproj != 0;
         if (perPixel[0].size() != (size_t)W * H || lastMaxBounces != opts.mMaxBounces) alloc();
         Ctx c; makeOptions(c);
         CamFrame cam = makeCamera(camIn, W, H);
@@ -2442,6 +2508,11 @@ int vro_set_volume(void* h, const vr_grid_view* views, int numViews, const vr_me
     for (int s = 0; s < VR_NUM_SLOTS; ++s) sc.slots[s] = oracle::Slot();
     for (int s = 0; s < numViews && s < VR_NUM_SLOTS; ++s)
         if (views[s].valid) load_slot(views[s], sc.slots[s]);
+    for (int s = 0; s < VR_NUM_SLOTS; ++s) p->staticSlots[s] = sc.slots[s];
+    p->anim.clear();
+    p->animId = -1;
+    sc.hasAnimation = false;
+    sc.hasVelocity = false;
     sc.med.sigma_s = mk3(m->sigma_s[0], m->sigma_s[1], m->sigma_s[2]);
     sc.med.sigma_a = mk3(m->sigma_a[0], m->sigma_a[1], m->sigma_a[2]);
     sc.med.sigma_t = m->sigma_s[0] + m->sigma_a[0];
@@ -2474,6 +2545,7 @@ int vro_set_lights(void* h, const vr_point_light* lights, int n, const vr_env_ma
 int vro_render_frame(void* h, const vr_camera* cam, float* out_rgba, float* mvec) {
     Oracle* p = (Oracle*)h;
     p->loopLimit = false;
+    p->animAdvance();
     p->renderFrame(*cam, out_rgba, mvec);
     return p->loopLimit ? VR_ERR_LOOP_LIMIT : VR_OK;
 }
@@ -2609,6 +2681,43 @@ void vro_set_emission(void* h, const vr_grid_view* tview, const float* lut, floa
     memcpy(e.lut, lut, sizeof(e.lut));
     e.leScale = leScale; e.cutoff = cutoff; e.scale = scale;
     e.has = true;
+    e.prevSlot = e.slot;          // a static grid is its own previous frame
+    e.lastHas = true;
+}
+
+// views: n * VR_NUM_SLOTS density slots; tviews: n temperature grids (valid = 0: no emission in
+// that frame) or NULL; vviews: 3n velocity components or NULL; the emission parameters apply to
+// the frames' temperature grids.  n = 0 returns to the static volume.
+void vro_set_animation(void* h, const vr_grid_view* views, int n, const vr_grid_view* tviews, const vr_grid_view* vviews, float vscale,
+                       const float* lut, float leScale, float cutoff, float scale) {
+    Oracle* p = (Oracle*)h;
+    oracle::Scene& sc = p->sc;
+    p->optionsChanged = true;
+    p->anim.clear();
+    p->animId = -1;
+    for (int k = 0; k < VR_NUM_SLOTS; ++k) { sc.slots[k] = p->staticSlots[k]; sc.slots[oracle::kPrevSlotOffset + k] = oracle::Slot(); }
+    sc.hasAnimation = false;
+    sc.hasVelocity = false;
+    for (int k = 0; k < 3; ++k) sc.vel[k] = oracle::Slot();
+    if (sc.emis.has) sc.emis.prevSlot = sc.emis.slot;
+    sc.emis.lastHas = sc.emis.has;
+    p->animTemp = tviews != nullptr;
+    p->animVel = vviews != nullptr;
+    p->animVelScale = vscale;
+    if (n <= 0) { p->animTemp = p->animVel = false; return; }
+    p->anim.resize(n);
+    for (int i = 0; i < n; ++i) {
+        Oracle::AnimFrame& f = p->anim[i];
+        for (int k = 0; k < VR_NUM_SLOTS; ++k)
+            if (views[(size_t)i * VR_NUM_SLOTS + k].valid) load_slot(views[(size_t)i * VR_NUM_SLOTS + k], f.slots[k]);
+        if (tviews && tviews[i].valid) { load_slot(tviews[i], f.temp); f.hasTemp = true; }
+        if (vviews)
+            for (int k = 0; k < 3; ++k) load_slot(vviews[3 * i + k], f.vel[k]);
+    }
+    if (tviews) {
+        memcpy(sc.emis.lut, lut, sizeof(sc.emis.lut));
+        sc.emis.leScale = leScale; sc.emis.cutoff = cutoff; sc.emis.scale = scale;
+    }
 }
 
 // learned target (test infrastructure)

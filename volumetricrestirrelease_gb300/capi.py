@@ -43,7 +43,7 @@ class Options(C.Structure):
         ("mFinalLightTrackingMethod", _u32), ("mFinalTStepScale", _f32),
         ("mUseLearnedPHat", _i32), ("mLearnedTrainSamples", _i32), ("mLearnedBatch", _i32),
         ("mLearnedLearningRate", _f32), ("mLearnedTFloor", _f32), ("mLearnedSeed", _u32),
-        ("mLearnedTargetMethod", _u32), ("mLearnedLoss", _i32),
+        ("mLearnedTargetMethod", _u32), ("mLearnedLoss", _i32), ("mUsePrevVolumeForReproj", _i32),
     ]
 
     def as_dict(self):
@@ -132,6 +132,9 @@ SIGNATURES = {
     "vr_selftest_rng": (_i32, [C.POINTER(_u32), _i32, _i32, C.POINTER(_f32)]),
     "vr_selftest_umma": (_i32, [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), C.POINTER(_f32), _i32]),
     "vr_set_block_size": (_i32, [_P, _i32]),
+    "vr_set_animation": (_i32, [_P, C.POINTER(_P), _i32, C.POINTER(_P), C.POINTER(_P), _f32]),
+    "vr_volume_create_dense_signed": (_i32, [_P, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
+    "vr_animation_frame": (_i32, [_P]),
     "vr_batch_create": (_i32, [C.POINTER(_P), _i32, C.POINTER(_P)]),
     "vr_batch_destroy": (None, [_P]),
     "vr_batch_last_error": (C.c_char_p, [_P]),

@@ -215,9 +215,24 @@ struct vr_context {
     std::vector<void*> sceneAllocs;
     bool hasVolume = false;
     int numMips = 0;
+    int staticRes = 0;
     std::vector<void*> envAllocs;
     std::vector<void*> emisAllocs;
     HostEnv env;
+    // emission parameters of the last vr_set_emission (the reference's defaults until then)
+    bool emisParamsSet = false;
+    // animated volume: every frame's grids resident, bound cyclically frame by frame
+    struct AnimFrame {
+        vrd::DevSlot slots[VR_NUM_SLOTS];
+        vrd::DevSlot temp, vel[3];
+        bool hasTemp = false;
+    };
+    std::vector<AnimFrame> anim;
+    std::vector<void*> animAllocs;
+    vrd::DevSlot staticSlots[VR_NUM_SLOTS]{};   // the volume of vr_set_volume
+    int animId = -1;
+    bool animTemp = false, animVel = false;
+    float animVelScale = 1.f;
     // buffers
     vrd::ResBuf res[3]{};      // 0 = perPixel[0], 1 = perPixel[1], 2 = temporal history
     float* feat[2] = {nullptr, nullptr};
@@ -452,6 +467,7 @@ static bool options_valid(const vr_options* o, std::string& why) {
                           o->mFinalVisibilityTrackingMethod, o->mFinalLightTrackingMethod};
     for (uint32_t m : methods) if (m > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown tracking method"; return false; }
     if (o->mTemporalReprojectionMode > VR_REPROJ_NO_BACKGROUND) { why = "unknown reprojection mode"; return false; }
+    if (o->mUsePrevVolumeForReproj != 0 && o->mUsePrevVolumeForReproj != 1) { why = "mUsePrevVolumeForReproj must be 0 or 1"; return false; }
     if (o->mUseLearnedPHat) {
         if (!o->mEnableTemporalReuse && !o->mEnableSpatialReuse) { why = "mUseLearnedPHat needs temporal or spatial reuse"; return false; }
         if (o->mLearnedTrainSamples < 0 || o->mLearnedTrainSamples > (1 << 26)) { why = "mLearnedTrainSamples must be in [0, 2^26]"; return false; }
@@ -558,6 +574,7 @@ void vr_options_default(vr_options* o) {
     o->mLearnedSeed = 1;
     o->mLearnedTargetMethod = VR_TRACK_RAY_MARCHING;
     o->mLearnedLoss = 0;
+    o->mUsePrevVolumeForReproj = 1;
 }
 
 // ---- volumes ----
@@ -584,6 +601,20 @@ int vr_volume_create_dense(const float* density, int32_t res, int32_t num_mips, 
         for (float& x : g) if (!(x >= 0.f) || vr::isinf_(x)) return VR_ERR_INVALID_ARG;
         vr_volume* v = new vr_volume();
         if (vr::build_volume(g, res, num_mips, world_min, voxel_size, fp16 != 0, v->v) != 0) { delete v; return VR_ERR_INVALID_ARG; }
+        *out = v;
+        return VR_OK;
+    } catch (...) {
+        return VR_ERR_OOM;
+    }
+}
+int vr_volume_create_dense_signed(const float* values, int32_t res, const float world_min[3], float voxel_size, int32_t fp16, vr_volume** out) {
+    if (!values || !out || !world_min) return VR_ERR_INVALID_ARG;
+    if (res <= 0 || res > 4096 || res % 8 != 0 || !(voxel_size > 0.f)) return VR_ERR_INVALID_ARG;
+    try {
+        std::vector<float> g(values, values + (size_t)res * res * res);
+        for (float& x : g) if (!(x == x) || vr::isinf_(x)) return VR_ERR_INVALID_ARG;
+        vr_volume* v = new vr_volume();
+        if (vr::build_signed_grid(g, res, world_min, voxel_size, fp16 != 0, v->v) != 0) { delete v; return VR_ERR_INVALID_ARG; }
         *out = v;
         return VR_OK;
     } catch (...) {
@@ -647,6 +678,7 @@ void vr_destroy(vr_context* c) {
     for (void* p : c->sceneAllocs) cudaFree(p);
     for (void* p : c->envAllocs) cudaFree(p);
     for (void* p : c->emisAllocs) cudaFree(p);
+    for (void* p : c->animAllocs) cudaFree(p);
     for (auto& e : c->ev) if (e) cudaEventDestroy(e);
     for (auto& v : c->pendingEv) for (auto e : v) cudaEventDestroy(e);
     for (auto e : c->freeEv) cudaEventDestroy(e);
@@ -711,7 +743,9 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
     for (void* p : c->emisAllocs) cudaFree(p);
     c->emisAllocs.clear();
     memset(&c->scene.tslot, 0, sizeof(c->scene.tslot));
+    memset(&c->scene.ptslot, 0, sizeof(c->scene.ptslot));
     c->scene.hasEmission = 0;
+    c->scene.lastHasEmission = 0;
     c->optionsChanged = true;
     if (!temp) return VR_OK;
     if (!(le_scale >= 0.f) || vr::isinf_(le_scale) || !(scale == scale) || !(cutoff == cutoff)) { c->err = "invalid emission parameters"; return VR_ERR_INVALID_ARG; }
@@ -725,6 +759,7 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
         return p;
     };
     vrd::DevSlot& d = c->scene.tslot;
+    c->emisParamsSet = true;
     d.valid = 1;
     d.res = g.res;
     d.bmaxf = (float)g.res;
@@ -746,11 +781,16 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
     c->scene.tCutoff = cutoff;
     c->scene.tScale = scale;
     c->scene.hasEmission = 1;
+    c->scene.ptslot = c->scene.tslot;          // a static grid is its own previous frame
+    c->scene.lastHasEmission = 1;
     return VR_OK;
 }
 
+static void anim_clear(vr_context* c);
+
 int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
     if (!c || !vol || !m) return VR_ERR_INVALID_ARG;
+    anim_clear(c);
     if (!(m->sigma_s[0] + m->sigma_a[0] > 0.f)) { c->err = "sigma_t must be positive"; return VR_ERR_INVALID_ARG; }
     if (m->sigma_s[0] + m->sigma_a[0] != m->sigma_s[1] + m->sigma_a[1] || m->sigma_s[1] + m->sigma_a[1] != m->sigma_s[2] + m->sigma_a[2]) {
         c->err = "sigma_t must be grey (sigma_s + sigma_a equal on all channels)"; return VR_ERR_INVALID_ARG;
@@ -793,14 +833,143 @@ int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
     c->scene.superDiag = v.supervoxel_diag;
     c->scene.numMips = v.num_mips;
     c->numMips = v.num_mips;
+    c->staticRes = v.res;
     for (int i = 0; i < 3; ++i) {
         c->netBmin[i] = v.world_min[i];
         c->netBinv[i] = 1.f / ((float)v.res * v.voxel_size);
     }
+    memcpy(c->staticSlots, c->scene.slots, sizeof(c->staticSlots));
     c->hasVolume = true;
     c->optionsChanged = true;
     return VR_OK;
 }
+
+// ---- animated volumes ----
+static bool upload_grid(const vr::GridSlot& g, vrd::DevSlot& d, std::vector<void*>& allocs) {
+    memset(&d, 0, sizeof(d));
+    if (!g.valid) return true;
+    auto up = [&](const void* src, size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        allocs.push_back(p);
+        if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+        return p;
+    };
+    d.valid = 1;
+    d.res = g.res;
+    d.bmaxf = (float)g.res;
+    d.maxValue = g.max_value;
+    memcpy(d.M, g.world_to_index, sizeof(d.M));
+    d.root = (const int*)up(g.root_child.data(), g.root_child.size() * 4);
+    d.l1vmin = (const int4*)up(g.l1_vmin.data(), g.l1_vmin.size() * 4);
+    d.l1child = (const int*)up(g.l1_child.data(), g.l1_child.size() * 4);
+    d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
+    d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
+    if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
+    else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+    return d.root && d.l1vmin && d.l1child && d.bvmin && d.bounds && (d.f32 || d.f16);
+}
+
+static void anim_clear(vr_context* c) {
+    if (c->anim.empty()) return;
+    cudaDeviceSynchronize();                 // frames in flight may still read the grids
+    for (void* p : c->animAllocs) cudaFree(p);
+    c->animAllocs.clear();
+    c->anim.clear();
+    c->animId = -1;
+    c->animTemp = c->animVel = false;
+    memcpy(c->scene.slots, c->staticSlots, sizeof(c->staticSlots));
+    memset(c->scene.slots + vrd::kPrevSlotOffset, 0, sizeof(vrd::DevSlot) * VR_NUM_SLOTS);
+    memset(c->scene.vslot, 0, sizeof(c->scene.vslot));
+    c->scene.hasAnimation = 0;
+    c->scene.hasVelocity = 0;
+    if (c->scene.hasEmission) c->scene.ptslot = c->scene.tslot;
+    c->scene.lastHasEmission = c->scene.hasEmission;
+}
+
+// Scene::update (Scene.cpp:825-860): the next animation frame becomes current, the one before
+// it supplies the previous-frame grids
+static void anim_advance(vr_context* c) {
+    if (c->anim.empty()) return;
+    const int n = (int)c->anim.size();
+    c->animId = (c->animId + 1) % n;
+    const int cur = c->animId, prv = (cur + n - 1) % n;
+    memcpy(c->scene.slots, c->anim[cur].slots, sizeof(c->anim[cur].slots));
+    memcpy(c->scene.slots + vrd::kPrevSlotOffset, c->anim[prv].slots, sizeof(c->anim[prv].slots));
+    c->scene.hasAnimation = 1;
+    if (c->animTemp) {
+        c->scene.tslot = c->anim[cur].temp;
+        c->scene.ptslot = c->anim[prv].temp;
+        c->scene.hasEmission = c->anim[cur].hasTemp;
+        c->scene.lastHasEmission = c->anim[prv].hasTemp;
+    }
+    if (c->animVel) {
+        memcpy(c->scene.vslot, c->anim[cur].vel, sizeof(c->scene.vslot));
+        c->scene.hasVelocity = 1;
+        c->scene.velocityScale = c->animVelScale;
+    }
+}
+
+// frames share the grid layout and voxel size (the tracking step and the brick structure);
+// each keeps its own world placement (its slots' world -> index transforms)
+static bool same_layout(const vr::Volume& a, const vr::Volume& b) {
+    return a.res == b.res && a.num_mips == b.num_mips && a.voxel_size == b.voxel_size;
+}
+
+int vr_set_animation(vr_context* c, const vr_volume* const* frames, int32_t n, const vr_volume* const* temperature,
+                     const vr_volume* const* velocity, float velocity_scale) {
+    if (!c || n < 0 || (n > 0 && !frames)) return VR_ERR_INVALID_ARG;
+    if (!c->hasVolume) { c->err = "no volume bound (vr_set_volume)"; return VR_ERR_STATE; }
+    anim_clear(c);
+    c->optionsChanged = true;
+    if (n == 0) return VR_OK;
+    if (!(velocity_scale == velocity_scale) || vr::isinf_(velocity_scale)) { c->err = "invalid velocity scale"; return VR_ERR_INVALID_ARG; }
+    const vr::Volume* base = nullptr;
+    for (int i = 0; i < n; ++i) {
+        if (!frames[i]) { c->err = "null animation frame"; return VR_ERR_INVALID_ARG; }
+        if (!base) base = &frames[i]->v;
+        if (!same_layout(*base, frames[i]->v) || base->res != c->staticRes || base->num_mips != c->numMips ||
+            base->voxel_size != c->scene.tStep) {
+            c->err = "animation frames need the res, mip count and voxel size of the bound volume"; return VR_ERR_INVALID_ARG;
+        }
+        if (temperature && temperature[i] && !temperature[i]->v.slots[0].valid) { c->err = "temperature grid has no mip 0"; return VR_ERR_INVALID_ARG; }
+        if (velocity)
+            for (int k = 0; k < 3; ++k)
+                if (!velocity[3 * i + k] || !velocity[3 * i + k]->v.slots[0].valid) { c->err = "velocity needs 3 grids per frame, each with mip 0"; return VR_ERR_INVALID_ARG; }
+    }
+    c->anim.resize(n);
+    bool ok = true;
+    for (int i = 0; i < n && ok; ++i) {
+        vr_context::AnimFrame& f = c->anim[i];
+        for (int sl = 0; sl < VR_NUM_SLOTS && ok; ++sl) ok = upload_grid(frames[i]->v.slots[sl], f.slots[sl], c->animAllocs);
+        if (ok && temperature && temperature[i]) { ok = upload_grid(temperature[i]->v.slots[0], f.temp, c->animAllocs); f.hasTemp = true; }
+        if (velocity)
+            for (int k = 0; k < 3 && ok; ++k) ok = upload_grid(velocity[3 * i + k]->v.slots[0], f.vel[k], c->animAllocs);
+    }
+    if (!ok) {
+        for (void* p : c->animAllocs) cudaFree(p);
+        c->animAllocs.clear();
+        c->anim.clear();
+        c->err = "out of device memory (animation)";
+        return VR_ERR_OOM;
+    }
+    c->animTemp = temperature != nullptr;
+    c->animVel = velocity != nullptr;
+    c->animVelScale = velocity_scale;
+    if (c->animTemp && !c->emisParamsSet) {
+        // Scene::addGVDBVolume defaults (Scene.h:481): LeScale 0.005, cutoff 1, scale 100
+        c->scene.leScale = 0.005f;
+        c->scene.tCutoff = 1.f;
+        c->scene.tScale = 100.f;
+        float tab[384];
+        vr::blackbody_lut(tab);
+        memcpy(c->scene.blackbody, tab, sizeof(tab));
+    }
+    c->animId = -1;
+    return VR_OK;
+}
+
+int32_t vr_animation_frame(const vr_context* c) { return c ? c->animId : -1; }
 
 int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const vr_env_map* env) {
     if (!c || n < 0 || n > vrd::kMaxLights || (n > 0 && !lights)) { if (c) c->err = "at most 64 point lights"; return VR_ERR_INVALID_ARG; }
@@ -921,6 +1090,8 @@ int vr_render_frame(vr_context* c, const vr_camera* cam, float* out_rgba, float*
     if (!c || !out_rgba) return VR_ERR_INVALID_ARG;
     int r = prepare_frame(c, cam);
     if (r) return r;
+    anim_advance(c);
+    c->scene.usePrevGrid = c->opts.mUsePrevVolumeForReproj != 0;
     cudaStream_t st = (cudaStream_t)stream;
     if ((r = upload_scene(c, st))) return r;
     const vr_options& o = c->opts;
@@ -1543,6 +1714,7 @@ int noalloc_prepare(vr_context* c, const vr_camera* cam, int32_t frame_index, No
         return VR_ERR_INVALID_ARG;
     }
     if (frame_index < 0) { c->err = "frame_index must be >= 0"; return VR_ERR_INVALID_ARG; }
+    if (!c->anim.empty()) { c->err = "vr_render_frame_noalloc does not play animated volumes"; return VR_ERR_INVALID_ARG; }
     std::string why;
     if (!slots_present(c, why)) { c->err = why; return VR_ERR_INVALID_ARG; }
     if (o.mUseAnalyticLights && c->scene.numLights == 0) { c->err = "mUseAnalyticLights needs at least one point light"; return VR_ERR_INVALID_ARG; }
@@ -1882,7 +2054,7 @@ int vr_set_block_size(vr_context* c, int32_t threads) {
 
 int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
     if (!ctxs || !out || n < 1 || n > 1024) return VR_ERR_INVALID_ARG;
-    for (int i = 0; i < n; ++i) if (!ctxs[i]) return VR_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) if (!ctxs[i] || !ctxs[i]->anim.empty()) return VR_ERR_INVALID_ARG;
     const vr_options& o0 = ctxs[0]->opts;
     if (o0.mUseReference) return VR_ERR_INVALID_ARG;
     for (int i = 1; i < n; ++i) {

@@ -245,8 +245,10 @@ static std::vector<float> conservative0(const std::vector<float>& src, int R) {
 // ---------------------------------------------------------------------------------------
 // brick grid for one slot
 // ---------------------------------------------------------------------------------------
+// signedValues: any nonzero voxel makes its brick active and values are stored as given
+// (velocity components); otherwise only positive voxels count (densities, temperatures)
 static void build_slot(GridSlot& s, const std::vector<float>& g, int R, const float wmin[3],
-                       float vsize, bool fp16) {
+                       float vsize, bool fp16, bool signedValues = false) {
     s.valid = 1;
     s.res = R;
     const int NB = R / 8;                    // bricks per axis
@@ -265,7 +267,8 @@ static void build_slot(GridSlot& s, const std::vector<float>& g, int R, const fl
                 for (int z = 0; z < 8 && !any; ++z)
                     for (int y = 0; y < 8 && !any; ++y)
                         for (int x = 0; x < 8; ++x)
-                            if (g[((size_t)(bz * 8 + z) * R + (by * 8 + y)) * R + (bx * 8 + x)] > 0.0f) { any = true; break; }
+                            if (signedValues ? g[((size_t)(bz * 8 + z) * R + (by * 8 + y)) * R + (bx * 8 + x)] != 0.0f
+                                             : g[((size_t)(bz * 8 + z) * R + (by * 8 + y)) * R + (bx * 8 + x)] > 0.0f) { any = true; break; }
                 active[((size_t)bz * NB + by) * NB + bx] = any ? 1 : 0;
             }
     });
@@ -330,7 +333,7 @@ static void build_slot(GridSlot& s, const std::vector<float>& g, int R, const fl
             for (int y = 0; y < 10; ++y)
                 for (int x = 0; x < 10; ++x) {
                     float v = at(vx + x - 1, vy + y - 1, vz + z - 1);
-                    if (maxv > 0.0f && (double)(v / maxv) < 1e-9) v = 0.0f;
+                    if (!signedValues && maxv > 0.0f && (double)(v / maxv) < 1e-9) v = 0.0f;
                     size_t o = (size_t)b * 1000 + (z * 10 + y) * 10 + x;
                     if (fp16) s.brick_f16[o] = float_to_half(v);
                     else s.brick_f32[o] = v;
@@ -345,6 +348,19 @@ static void build_slot(GridSlot& s, const std::vector<float>& g, int R, const fl
     s.world_to_index[13] = -wmin[1] * inv;
     s.world_to_index[14] = -wmin[2] * inv;
     s.world_to_index[15] = 1.0f;
+}
+
+int build_signed_grid(const std::vector<float>& dense, int R, const float wmin[3], float vsize, bool fp16, Volume& vol) {
+    if (R <= 0 || R % 8 != 0 || R > 4096) return 1;
+    vol.res = R;
+    vol.num_mips = 1;
+    vol.voxel_size = vsize;
+    vol.fp16 = fp16 ? 1 : 0;
+    for (int i = 0; i < 3; ++i) vol.world_min[i] = wmin[i];
+    vol.supervoxel_diag = 8.0f * sqrt_(vsize * vsize + vsize * vsize + vsize * vsize);
+    for (auto& s : vol.slots) s = GridSlot();
+    build_slot(vol.slots[0], dense, R, wmin, vsize, fp16, true);
+    return 0;
 }
 
 int build_volume(const std::vector<float>& dense, int R, int numMips, const float wmin[3],

@@ -55,8 +55,13 @@ struct DevSlot {
     const __half* f16;
 };
 
+// slots [0, VR_NUM_SLOTS): the current frame's mips (normal, then conservative); with an
+// animated volume, [kPrevSlotOffset, kPrevSlotOffset + VR_NUM_SLOTS) hold the previous animation
+// frame's (the reference's kPrevFrameDensityGridOffset, HostDeviceSharedConstants.slang:27)
+constexpr int kPrevSlotOffset = VR_NUM_SLOTS;
+
 struct DevScene {
-    DevSlot slots[VR_NUM_SLOTS];
+    DevSlot slots[2 * VR_NUM_SLOTS];
     float sigma_t;
     f3 sigma_s, sigma_a;
     float g;
@@ -81,6 +86,12 @@ struct DevScene {
     DevSlot tslot;
     float leScale, tCutoff, tScale;
     float blackbody[128][3];     // radiance of 50 K .. 6400 K in steps of 50 K (texel centres)
+    // animated volumes (VolumeDesc.hasAnimation, usePrevGridForReproj, lastFrameHasEmission,
+    // hasVelocity, velocityScale; SceneTypes.slang:101-109)
+    int hasAnimation, usePrevGrid, lastHasEmission, hasVelocity;
+    float velocityScale;
+    DevSlot ptslot;              // the previous animation frame's temperature grid
+    DevSlot vslot[3];            // velocity components (world units per frame), mip 0
 };
 
 struct SamplingOptions {         // HostDeviceSharedDefinitions.h:96-141
@@ -327,8 +338,8 @@ static __device__ __noinline__ float densityWorld(f3 pw, int mip) {
 // Temperature / ConvertTempToColor / EmissionWorldSpace (VolumeBase.slang:196-232): trilinear
 // temperature at mip 0, mapped to a blackbody colour through the 128-texel table with linear
 // filtering between texel centres and clamped addressing
-static __device__ __noinline__ float temperatureWorld(f3 pw) {
-    const DevSlot& s = c_scene.tslot;
+static __device__ __noinline__ float temperatureWorld(f3 pw, bool last) {
+    const DevSlot& s = last ? c_scene.ptslot : c_scene.tslot;
     f3 p = mulPoint(pw, s.M);
     if (p.x < 0.f || p.y < 0.f || p.z < 0.f || p.x >= s.bmaxf || p.y >= s.bmaxf || p.z >= s.bmaxf) return 0.f;
     f3 vmin;
@@ -349,9 +360,25 @@ __device__ inline f3 tempToColor(float temp) {
     const f3 b = mk3(c_scene.blackbody[i1][0], c_scene.blackbody[i1][1], c_scene.blackbody[i1][2]);
     return c_scene.leScale * (a + (b - a) * f);
 }
-static __device__ __noinline__ f3 emissionWorld(f3 pw) {
-    if (!c_scene.hasEmission) return mk3(0.f);
-    return tempToColor(temperatureWorld(pw));
+static __device__ __noinline__ f3 emissionWorld(f3 pw, bool last = false) {
+    if (last ? !c_scene.lastHasEmission : !c_scene.hasEmission) return mk3(0.f);
+    return tempToColor(temperatureWorld(pw, last));
+}
+// VelocityWorld (VolumeBase.slang:182-194): the trilinear velocity at mip 0, zero outside the
+// grids (the points given may be far outside: the comparisons also reject NaN)
+static __device__ __noinline__ f3 velocityWorld(f3 pw) {
+    float v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const DevSlot& s = c_scene.vslot[k];
+        const f3 p = mulPoint(pw, s.M);
+        v[k] = 0.f;
+        if (!(p.x >= 0.f && p.y >= 0.f && p.z >= 0.f && p.x < s.bmaxf && p.y < s.bmaxf && p.z < s.bmaxf)) continue;
+        f3 vmin;
+        const int br = findBrick(s, p, vmin);
+        if (br >= 0) v[k] = trilinearIn(s, br, p - vmin);
+    }
+    return mk3(v[0], v[1], v[2]);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -795,7 +822,8 @@ __device__ inline float trAnalytic(const Ray& r, int mip, vr::Rng& sg, bool lin)
     return a.Tr;
 }
 __device__ inline float trRayMarch(const Ray& r, int mip, bool lin, float tss, vr::Rng& sg) {
-    int eff = mip >= kNumMaxMips ? mip - kNumMaxMips : mip;
+    int eff = mip >= kPrevSlotOffset ? mip - kPrevSlotOffset : mip;
+    eff = eff >= kNumMaxMips ? eff - kNumMaxMips : eff;
     TrRayMarch a; a.lin = lin; a.tStep = c_scene.tStep * tss * (float)(eff + 1);
     trackVolume(r, mip, sg, a, false);
     return a.Tr;
@@ -1010,7 +1038,8 @@ __device__ inline f3 sampleDirectLighting(vr::Rng& sg, float& pdf, const MediumI
 // ---------------------------------------------------------------------------------------
 // path contribution re-evaluation (ReSTIRHelper.slang:91-496)
 // ---------------------------------------------------------------------------------------
-__device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, float uv0, float uv1, vr::Rng& sg, const SamplingOptions& o, bool cull) {
+__device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, float uv0, float uv1, vr::Rng& sg, const SamplingOptions& o, bool cull,
+                                       int off) {
     Ray sr;
     f3 Ld;
     if (lid < 0) {
@@ -1025,13 +1054,17 @@ __device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, flo
     } else {
         return mk3(0.f);
     }
-    float Tr = computeVisibility(sr, sg, o.lightSamples, cull ? o.lightingMipLevel : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
+    float Tr = computeVisibility(sr, sg, o.lightSamples, cull ? o.lightingMipLevel + off : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
     return Tr * Ld;
 }
 
-// extra: the extra-bounce plane base, indexed extra[b * N + tap.startPixel]
+// extra: the extra-bounce plane base, indexed extra[b * N + tap.startPixel]; lastFrame: the
+// sample as of the previous frame (the temporal tap's MIS weight), on the previous animation
+// frame's grids when the volume is animated and usePrevGrid is set
 static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* extra, int N, Ray ray, vr::Rng& sg, const SamplingOptions& o,
-                               int maxBounces, bool noReuse, bool isFinal) {
+                               int maxBounces, bool noReuse, bool isFinal, bool lastFrame = false) {
+    const bool useLast = lastFrame && c_scene.usePrevGrid && c_scene.hasAnimation;
+    const int off = useLast ? kPrevSlotOffset : 0;
     bool isBg = tap.depth == kRayTMax;
     ray.tMax = tap.depth;
     f3 F = mk3(1.f);
@@ -1041,10 +1074,10 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
     f3 pW = at(ray, ray.tMax);
     MediumInteraction mi{at(ray, ray.tMax), -ray.d, c_scene.g, true};
     {
-        float density = (isBg || noReuse) ? 1.f : densityWorld(pW, 0);
+        float density = (isBg || noReuse) ? 1.f : densityWorld(pW, off);
         if (density == 0.f) return mk3(0.f);
         if (!noReuse)
-            visibility = computeVisibility(ray, sg, o.visibilitySamples, o.visibilityMipLevel, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
+            visibility = computeVisibility(ray, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
         f3 sig = isBg ? mk3(1.f) : (isSelfEmission ? c_scene.sigma_a : c_scene.sigma_s);
         if (noReuse && !isBg) sig = sig / c_scene.sigma_t;
         F = F * (visibility * density * sig);
@@ -1053,7 +1086,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
         if (isBg) {
             F = F * envEval(ray.d);
         } else if (isSelfEmission) {
-            F = F * emissionWorld(pW);
+            F = F * emissionWorld(pW, useLast);
         } else {
             bool scatterEm = false;
             Ray sr{};
@@ -1084,7 +1117,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
                     f3 sig; float sd;
                     if (!noReuse) {
                         sig = curEm ? c_scene.sigma_a : c_scene.sigma_s;
-                        sd = vr::fmax_(0, densityWorld(pW, 0));
+                        sd = vr::fmax_(0, densityWorld(pW, off));
                     } else {
                         sig = curEm ? c_scene.sigma_a / c_scene.sigma_t : c_scene.sigma_s / c_scene.sigma_t;
                         sd = 1.f;
@@ -1094,23 +1127,24 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
                     if (vr::all_eq0(F)) return mk3(0.f);
                     float sv = 1.f;
                     if (!noReuse)
-                        sv = computeVisibility(sr, sg, o.visibilitySamples, o.visibilityMipLevel, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
+                        sv = computeVisibility(sr, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
                     F = F * sv;
                     mi.wo = -sr.d;
                     mi.p = pW;
                     if (vr::all_eq0(F)) return mk3(0.f);
                 }
-                if (scatterEm) F = F * emissionWorld(pW);
+                if (scatterEm) F = F * emissionWorld(pW, useLast);
                 else mi = MediumInteraction{at(sr, sr.tMax), -sr.d, c_scene.g, true};
             }
             if (!scatterEm && vr::any_gt0(F))
-                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal);
+                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal, off);
         }
     }
     return F;
 }
-__device__ __forceinline__ float evalPHat(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o, int mb) {
-    return vr::luminance(evaluateF(tap, extra, N, ray, sg, o, mb, false, false));
+__device__ __forceinline__ float evalPHat(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o, int mb,
+                                         bool lastFrame = false) {
+    return vr::luminance(evaluateF(tap, extra, N, ray, sg, o, mb, false, false, lastFrame));
 }
 __device__ __forceinline__ void resampleNeighbor(Reservoir& tap, const Ray& ray, vr::Rng& sg, const float4* extra, int N, const SamplingOptions& o, int mb) {
     if (tap.runningSum == 0.f) return;

@@ -239,6 +239,12 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
         if (rd == kRayTMax && P.reprojMode != VR_REPROJ_NO_BACKGROUND && !isBgRes)
             rd = rejectionSampleByDensity(ray, sg, kNumMaxMips + P.reprojMip);
         f3 p = ray.o + ray.d * rd;
+        // the point's position in the previous frame, from the velocity grid (a background point
+        // keeps its pixel below, so it needs none)
+        if (c_scene.hasVelocity && c_scene.hasAnimation && rd != kRayTMax) {
+            const f3 v = velocityWorld(p) * c_scene.velocityScale;
+            p = p - v;
+        }
         float in4[4] = {p.x, p.y, p.z, 1.f}, vp[4], cp[4];
         mulMat4(P.prevView, in4, vp);
         mulMat4(P.prevProj, vp, cp);
@@ -302,7 +308,7 @@ static __device__ __noinline__ void temporalReuse(const FrameParams& P, const Fr
                     Ray nr{P.prevPos, vr::normalize(pinholeDir(P.prevU, P.prevV, P.prevW, rx, ry, W, H)), 0, i == 0 ? cPrevDepth : tOrigDepth};
                     Reservoir tt = taps[i];
                     tt.depth = nr.tMax;
-                    float p_y = evalPHat(tt, i == 0 ? B.cur.extra : B.hist.extra, N, nr, sg, P.spatial, MB);
+                    float p_y = evalPHat(tt, i == 0 ? B.cur.extra : B.hist.extra, N, nr, sg, P.spatial, MB, true);
                     if (vr::isinf_(p_y) || vr::isnan_(p_y)) p_y = 0.f;
                     p_sum += p_y * cm;
                 }

@@ -32,6 +32,8 @@ struct Volume {
 uint16_t float_to_half(float f);
 float half_to_float(uint16_t h);
 std::vector<float> procedural_density(const vr_procedural_desc& d);
+// mip 0 only, values kept with their sign (bricks where any voxel is nonzero): velocity grids
+int build_signed_grid(const std::vector<float>& dense, int R, const float wmin[3], float vsize, bool fp16, Volume& vol);
 int build_volume(const std::vector<float>& dense, int R, int numMips, const float wmin[3],
                  float vsize, bool fp16, Volume& vol);
 void slot_view(const GridSlot& s, vr_grid_view* v);

@@ -48,6 +48,20 @@ class Volume:
         return cls(hd, lib), cls(ht, lib)
 
     @classmethod
+    def signed(cls, values, world_min, voxel_size, fp16=False, lib=None):
+        """Signed scalar grid, mip 0 only (a velocity component)."""
+        lib = lib or capi.load()
+        d = np.ascontiguousarray(values, dtype=np.float32)
+        assert d.ndim == 3 and d.shape[0] == d.shape[1] == d.shape[2]
+        wm = (C.c_float * 3)(*world_min)
+        h = C.c_void_p()
+        r = lib.vr_volume_create_dense_signed(d.ctypes.data_as(C.POINTER(C.c_float)), d.shape[0], wm, voxel_size,
+                                              1 if fp16 else 0, C.byref(h))
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_create_dense_signed failed ({r})")
+        return cls(h, lib)
+
+    @classmethod
     def dense(cls, density, world_min, voxel_size, num_mips=4, fp16=False, lib=None):
         lib = lib or capi.load()
         d = np.ascontiguousarray(density, dtype=np.float32)
@@ -153,6 +167,28 @@ class VolumetricReSTIR:
             lp = self._lut.ctypes.data_as(C.POINTER(C.c_float))
         self._check(self._lib.vr_set_emission(self._h, temperature._h if temperature is not None else None, le_scale, cutoff,
                                               scale, lp))
+
+    def set_animation(self, frames, temperature=None, velocity=None, velocity_scale=1.0):
+        """Animated volume sequence (Scene::addGVDBVolumeSequence): frames are Volumes with the
+        bound volume's res, box and mips; temperature one Volume (or None) per frame; velocity
+        three component Volumes per frame (x, y, z; world units per frame).  Each execute()
+        advances one frame, cyclically.  An empty list returns to the static volume."""
+        n = len(frames)
+        self._anim_keep = list(frames) + [t for t in (temperature or []) if t is not None] + list(velocity or [])
+        fa = (C.c_void_p * max(1, n))(*[f._h for f in frames])
+        ta = va = None
+        if temperature is not None:
+            if len(temperature) != n:
+                raise ValueError("one temperature entry per frame")
+            ta = (C.c_void_p * n)(*[t._h if t is not None else None for t in temperature])
+        if velocity is not None:
+            if len(velocity) != 3 * n:
+                raise ValueError("three velocity components per frame")
+            va = (C.c_void_p * (3 * n))(*[v._h for v in velocity])
+        self._check(self._lib.vr_set_animation(self._h, fa, n, ta, va, velocity_scale))
+
+    def animation_frame(self):
+        return int(self._lib.vr_animation_frame(self._h))
 
     def execute(self, camera, out_ptr, mvec_ptr=None, stream=0):
         """Renders one frame into device memory (width*height float4)."""

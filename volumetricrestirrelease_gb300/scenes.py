@@ -49,6 +49,8 @@ class SceneDesc:
     frames: int = 16
     fire: tuple = None             # (t_min, t_max, le_scale, cutoff, scale) for emissive plumes
     orbit_start_deg: float = 0.0
+    anim_frames: int = 0           # animated volume: number of frames in the cycle
+    anim_shift: tuple = None       # world displacement of the volume per animation frame
 
     def camera(self, frame=0):
         ang = math.radians(self.orbit_start_deg + self.orbit_deg_per_frame * frame)
@@ -199,6 +201,50 @@ def batch(n=32, fires=8, seed=2024, learned=True, fp16=True, scale=1.0):
         sc.orbit_start_deg = ang
         out.append(sc)
     return out
+
+
+def animated(width=128, height=96, frames=4, fp16=False, fire=False, shift_voxels=(1.5, 0.0, 0.75), res=64):
+    """A drifting cloud (or fire plume): the same procedural volume displaced by a fixed world
+    offset per animation frame, with a velocity grid equal to that offset.  Use make_animation."""
+    voxel = 1.0 / res
+    light = capi.PointLight()
+    light.pos[:] = [2.0, 2.0, 2.0]
+    light.intensity[:] = [50.0, 50.0, 50.0]
+    shift = tuple(v * voxel for v in shift_voxels)
+    fire_params = (500.0, 3000.0, 0.02, 0.0, 1.0) if fire else None
+    return SceneDesc(
+        name="animated_fire" if fire else "animated", width=width, height=height,
+        volume=_procedural(0, res, 3, 5, 0.0, (-0.5, -0.5, -0.5), voxel, fp16=fp16, num_mips=3),
+        medium=_medium(20.0, 0.9, 0.2), lights=[light], env_rgb=constant_env(0.2),
+        options=dict(mMaxBounces=2, mInitialM=6, mEnableTemporalReuse=1, mEnableSpatialReuse=1, mSpatialSampleCount=4,
+                     mSampleRadius=8.0, mUseAnalyticLights=1, mUseEnvironmentLights=1),
+        camera_radius=2.0, frames=2 * frames + 1, fire=fire_params, anim_frames=frames, anim_shift=shift)
+
+
+def make_animation(sc, lib=None):
+    """(frames, temperatures or None, velocity components) for an animated SceneDesc: frame i is
+    the scene's volume with its world_min moved by i * anim_shift; velocity is anim_shift everywhere
+    in the frame's box."""
+    import ctypes as C
+    from .restir import Volume
+    lib = lib or capi.load()
+    frames, temps, vels = [], [], []
+    d = sc.volume
+    for i in range(sc.anim_frames):
+        di = capi.ProceduralDesc()
+        C.pointer(di)[0] = d
+        for k in range(3):
+            di.world_min[k] = d.world_min[k] + i * sc.anim_shift[k]
+        if sc.fire:
+            dv, tv = Volume.fire(di, sc.fire[0], sc.fire[1], lib=lib)
+            frames.append(dv)
+            temps.append(tv)
+        else:
+            frames.append(Volume.procedural(di, lib=lib))
+        for k in range(3):
+            g = np.full((d.res, d.res, d.res), sc.anim_shift[k], np.float32)
+            vels.append(Volume.signed(g, tuple(di.world_min), d.voxel_size, lib=lib))
+    return frames, (temps if sc.fire else None), vels
 
 
 def make_volumes(sc, lib=None):
