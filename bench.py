@@ -453,6 +453,74 @@ def run_small_configs(args, lib):
     return res
 
 
+def run_animated(args, lib):
+    """Animated volume: a 128^3 cloud drifting 1.5 voxels per frame over 16 frames (no wrap of the
+    sequence inside the measured frames), 256^2, plain FP32, temporal + spatial, static camera.
+    frames/s against the same scene held static (each after 3 untimed frames), and relMSE
+    (frames 8..15) of the temporal pass with the previous-frame grids and velocity reprojection,
+    with velocity only, and with neither, each frame against a 1024-spp FP64 reference of that
+    frame's volume."""
+    import torch
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
+    W = H = 256
+    NF = 16
+    sc = scenes.animated(width=W, height=H, frames=NF, res=128)
+    frames, temps, vels = scenes.make_animation(sc, lib)
+    base = Volume.procedural(sc.volume, lib=lib)
+
+    def ctx(over=None, anim=True, velocity=True):
+        o = _options(lib, sc)
+        for k, v in (over or {}).items():
+            setattr(o, k, v)
+        r = VolumetricReSTIR(W, H, o.as_dict(), lib=lib)
+        r.setScene(base, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        if anim:
+            r.set_animation(frames, temps, vels if velocity else None, 1.0)
+        return r
+    out = torch.empty((H, W, 4), device="cuda")
+    refs = {}
+    rr = ctx()
+    for f in range(NF):
+        rr.execute(sc.camera(f), out.data_ptr())             # binds animation frame f
+        if f >= 8:
+            acc = torch.zeros((H, W, 3), device="cuda", dtype=torch.float64)
+            for f0 in range(0, 1024, 256):
+                rr.render_reference(sc.camera(f), acc.data_ptr(), f0, 256)
+            torch.cuda.synchronize()
+            refs[f] = (acc / 1024).cpu().numpy()
+    del rr
+    res = {"workload": "256^2, 128^3 cloud drifting 1.5 voxels per frame over 16 frames, plain FP32, temporal + 3 spatial "
+                       "neighbours, static camera; relMSE frames 8..15 against a 1024-spp FP64 reference of each frame's volume"}
+    for name, over, anim, velocity in (("static", {}, False, False), ("prev_grid_and_velocity", {}, True, True),
+                                       ("velocity_only", dict(mUsePrevVolumeForReproj=0), True, True),
+                                       ("neither", dict(mUsePrevVolumeForReproj=0), True, False)):
+        r = ctx(over, anim, velocity)
+        for f in range(3):
+            r.execute(sc.camera(f), out.data_ptr())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for f in range(3, NF):
+            r.execute(sc.camera(f), out.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        fps = (NF - 3) * 1000.0 / e0.elapsed_time(e1)
+        if name == "static":
+            res["static_frames_per_s"] = fps
+            continue
+        r2 = ctx(over, anim, velocity)
+        errs = []
+        for f in range(NF):
+            r2.execute(sc.camera(f), out.data_ptr())
+            if f >= 8:
+                torch.cuda.synchronize()
+                errs.append(_relmse(out.cpu().numpy(), refs[f]))
+        res[name] = {"frames_per_s": fps, "relmse_frames_8_15": float(np.mean(errs))}
+        del r, r2
+    return res
+
+
 def run_gpu(args):
     import torch
     ws, rank = _dist()
@@ -547,6 +615,9 @@ def run_gpu(args):
     small = None
     if not args.no_small and rank == 0:
         small = run_small_configs(args, lib)
+    animated = None
+    if not args.no_animated and rank == 0:
+        animated = run_animated(args, lib)
 
     if rank != 0:
         return
@@ -600,6 +671,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "batched": batched,
             "small_configs": small,
+            "animated": animated,
             "clocks": clocks}
     print(json.dumps(line), flush=True)
 
@@ -616,6 +688,7 @@ def main():
     ap.add_argument("--no-quality", action="store_true", help="skip the relMSE matching (learned form at M=32)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 32-instance form")
     ap.add_argument("--no-small", action="store_true", help="skip the 256^2 configurations (cfg1, cfg3, cfg4)")
+    ap.add_argument("--no-animated", action="store_true", help="skip the animated-volume measurement")
     ap.add_argument("--batch-steps", type=int, default=4)
     ap.add_argument("--batch-trials", type=int, default=6)
     args = ap.parse_args()

@@ -178,6 +178,7 @@ typedef struct vr_volume_info {
     int32_t num_bricks[VR_NUM_SLOTS];
     int64_t device_bytes;         /* bytes the grid occupies once bound to a context */
     int32_t fp16;
+    float world_min[3];           /* world position of index-space corner (0, 0, 0) */
 } vr_volume_info;
 
 typedef struct vr_point_light {   /* LightHelpers.slang:223-242 (point light, uniform emission) */
@@ -225,6 +226,21 @@ int vr_volume_create_procedural(const vr_procedural_desc* d, vr_volume** out);
 int vr_volume_create_dense(const float* density, int32_t res, int32_t num_mips,
                            const float world_min[3], float voxel_size, int32_t fp16,
                            vr_volume** out);
+/* GVDB .vbx files (gvdb-voxel-src/GVDB_FILESPEC.txt; VolumeGVDB::LoadVBX,
+ * gvdb_volume_gvdb.cpp:532-700; the files Scene::addGVDBVolume reads, Scene.cpp:2754-3058).
+ * Load reads grid 0 (float, one component, uncompressed, GVDB topology, atlas layout, 8^3
+ * leaves, no rotation, uniform scale; versions 1.0-2.x), walks its tree from the root and builds
+ * num_mips normal and conservative mips from the reachable leaves, over the file's effective
+ * voxel box (version x.12) or the leaves' box; world = (index + pretranslation) * scale +
+ * translation.  flags: VR_VBX_FP16 stores FP16 bricks; VR_VBX_SIGNED keeps signed values, mip 0
+ * only (velocity components).  Grids up to 1024^3 voxels.  Save writes mip 0 of a volume as a
+ * version 1.12 file in the three-level layout (log2 dims 3, 4, 5) with a one-voxel apron.
+ * vr_volume_vbx_error describes the last failure of either on this thread. */
+#define VR_VBX_FP16 1
+#define VR_VBX_SIGNED 2
+int vr_volume_load_vbx(const char* path, int32_t num_mips, int32_t flags, vr_volume** out);
+int vr_volume_save_vbx(const vr_volume* v, const char* path);
+const char* vr_volume_vbx_error(void);
 /* A signed scalar grid, mip 0 only (velocity components for vr_set_animation): bricks wherever
  * a voxel is nonzero, values stored as given.  values: res^3, x fastest. */
 int vr_volume_create_dense_signed(const float* values, int32_t res, const float world_min[3], float voxel_size,

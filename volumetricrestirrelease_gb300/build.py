@@ -74,6 +74,10 @@ def build(force=False, jobs=None):
     src = CSRC / "volume.cpp"
     units.append((obj, [src] + hdrs, ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math",
                                       "-c", str(src), "-o", str(obj)]))
+    obj = BUILD / "vbx.o"
+    src = CSRC / "vbx.cpp"
+    units.append((obj, [src] + hdrs, ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math",
+                                      "-c", str(src), "-o", str(obj)]))
     todo = [(o, c) for (o, s, c) in units if force or _stale(o, s)]
     with cf.ThreadPoolExecutor(max_workers=jobs or max(1, min(len(todo), os.cpu_count() or 4))) as ex:
         futs = [ex.submit(_run, c, o.with_suffix(".log")) for (o, c) in todo]

@@ -70,7 +70,7 @@ class GridView(C.Structure):
 
 class VolumeInfo(C.Structure):
     _fields_ = [("num_mips", _i32), ("res", _i32), ("voxel_size", _f32), ("supervoxel_diag", _f32),
-                ("num_bricks", _i32 * VR_NUM_SLOTS), ("device_bytes", C.c_int64), ("fp16", _i32)]
+                ("num_bricks", _i32 * VR_NUM_SLOTS), ("device_bytes", C.c_int64), ("fp16", _i32), ("world_min", _f32 * 3)]
 
 
 class PointLight(C.Structure):
@@ -134,6 +134,9 @@ SIGNATURES = {
     "vr_set_block_size": (_i32, [_P, _i32]),
     "vr_set_animation": (_i32, [_P, C.POINTER(_P), _i32, C.POINTER(_P), C.POINTER(_P), _f32]),
     "vr_volume_create_dense_signed": (_i32, [_P, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
+    "vr_volume_load_vbx": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(_P)]),
+    "vr_volume_save_vbx": (_i32, [_P, C.c_char_p]),
+    "vr_volume_vbx_error": (C.c_char_p, []),
     "vr_animation_frame": (_i32, [_P]),
     "vr_batch_create": (_i32, [C.POINTER(_P), _i32, C.POINTER(_P)]),
     "vr_batch_destroy": (None, [_P]),

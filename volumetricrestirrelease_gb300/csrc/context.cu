@@ -621,6 +621,48 @@ int vr_volume_create_dense_signed(const float* values, int32_t res, const float 
         return VR_ERR_OOM;
     }
 }
+static thread_local std::string g_vbxErr;
+int vr_volume_load_vbx(const char* path, int32_t num_mips, int32_t flags, vr_volume** out) {
+    g_vbxErr.clear();
+    if (!path || !out || num_mips < 1 || num_mips > VR_NUM_MAX_MIPS || (flags & ~(VR_VBX_FP16 | VR_VBX_SIGNED))) { g_vbxErr = "invalid argument"; return VR_ERR_INVALID_ARG; }
+    try {
+        FILE* fp = fopen(path, "rb");
+        if (!fp) { g_vbxErr = std::string("cannot open ") + path; return VR_ERR_INVALID_ARG; }
+        std::vector<unsigned char> file;
+        unsigned char buf[1 << 16];
+        size_t k;
+        while ((k = fread(buf, 1, sizeof(buf), fp)) > 0) file.insert(file.end(), buf, buf + k);
+        fclose(fp);
+        vr_volume* v = new vr_volume();
+        if (vr::read_vbx(file, (flags & VR_VBX_SIGNED) ? 1 : num_mips, (flags & VR_VBX_FP16) != 0, (flags & VR_VBX_SIGNED) != 0, v->v, g_vbxErr) != 0) {
+            delete v;
+            return VR_ERR_INVALID_ARG;
+        }
+        *out = v;
+        return VR_OK;
+    } catch (...) {
+        g_vbxErr = "out of host memory";
+        return VR_ERR_OOM;
+    }
+}
+int vr_volume_save_vbx(const vr_volume* v, const char* path) {
+    g_vbxErr.clear();
+    if (!v || !path) { g_vbxErr = "invalid argument"; return VR_ERR_INVALID_ARG; }
+    try {
+        std::vector<unsigned char> file;
+        if (vr::write_vbx(v->v, file, g_vbxErr) != 0) return VR_ERR_INVALID_ARG;
+        FILE* fp = fopen(path, "wb");
+        if (!fp) { g_vbxErr = std::string("cannot create ") + path; return VR_ERR_INVALID_ARG; }
+        const bool ok = fwrite(file.data(), 1, file.size(), fp) == file.size();
+        fclose(fp);
+        if (!ok) { g_vbxErr = "write failed"; return VR_ERR_INVALID_ARG; }
+        return VR_OK;
+    } catch (...) {
+        g_vbxErr = "out of host memory";
+        return VR_ERR_OOM;
+    }
+}
+const char* vr_volume_vbx_error(void) { return g_vbxErr.c_str(); }
 void vr_volume_destroy(vr_volume* v) { delete v; }
 int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
     if (!v || !info) return VR_ERR_INVALID_ARG;
@@ -630,6 +672,7 @@ int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
     info->voxel_size = v->v.voxel_size;
     info->supervoxel_diag = v->v.supervoxel_diag;
     info->fp16 = v->v.fp16;
+    for (int i = 0; i < 3; ++i) info->world_min[i] = v->v.world_min[i];
     int64_t bytes = 0;
     for (int s = 0; s < VR_NUM_SLOTS; ++s) {
         const vr::GridSlot& g = v->v.slots[s];

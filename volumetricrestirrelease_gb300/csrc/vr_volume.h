@@ -1,6 +1,7 @@
 // vr_volume.h -- host-side sparse brick grid (internal to libvrestir).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "../../include/vrestir.h"
@@ -37,6 +38,9 @@ int build_signed_grid(const std::vector<float>& dense, int R, const float wmin[3
 int build_volume(const std::vector<float>& dense, int R, int numMips, const float wmin[3],
                  float vsize, bool fp16, Volume& vol);
 void slot_view(const GridSlot& s, vr_grid_view* v);
+// GVDB .vbx files (vbx.cpp)
+int read_vbx(const std::vector<unsigned char>& file, int numMips, bool fp16, bool signedValues, Volume& vol, std::string& err);
+int write_vbx(const Volume& vol, std::vector<unsigned char>& out, std::string& err);
 void blackbody_lut(float rgb[384]);
 void procedural_fire(const vr_procedural_desc& d, float t_min, float t_max, std::vector<float>& density, std::vector<float>& temperature);
 

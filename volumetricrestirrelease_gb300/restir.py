@@ -48,6 +48,22 @@ class Volume:
         return cls(hd, lib), cls(ht, lib)
 
     @classmethod
+    def load_vbx(cls, path, num_mips=4, fp16=False, signed=False, lib=None):
+        """A GVDB .vbx file (grid 0); signed: a velocity component (mip 0 only)."""
+        lib = lib or capi.load()
+        h = C.c_void_p()
+        flags = (1 if fp16 else 0) | (2 if signed else 0)
+        r = lib.vr_volume_load_vbx(str(path).encode(), num_mips, flags, C.byref(h))
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_load_vbx failed ({r}): {lib.vr_volume_vbx_error().decode()}")
+        return cls(h, lib)
+
+    def save_vbx(self, path):
+        r = self._lib.vr_volume_save_vbx(self._h, str(path).encode())
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_save_vbx failed ({r}): {self._lib.vr_volume_vbx_error().decode()}")
+
+    @classmethod
     def signed(cls, values, world_min, voxel_size, fp16=False, lib=None):
         """Signed scalar grid, mip 0 only (a velocity component)."""
         lib = lib or capi.load()
@@ -112,6 +128,26 @@ def env_struct(rgb, scale=(1.0, 1.0, 1.0), rotation=None):
     e.scale[:] = list(scale)
     e.rotation[:] = list(rotation) if rotation is not None else [1, 0, 0, 0, 1, 0, 0, 0, 1]
     return e, rgb
+
+
+def load_gvdb_volume(vbx, num_mips=1, fp16=False, lib=None):
+    """The file layout Scene::addGVDBVolume reads (Scene.cpp:2769-2816): with num_mips > 1, `vbx`
+    is a folder <dir>/<name> holding <name>_mip0.vbx (this loader rebuilds the finer mips and the
+    conservative <name>_mip<k>c.vbx from mip 0); with num_mips == 1 it is the file itself.
+    <name>_temperature.vbx and <name>_velocity_{x,y,z}.vbx in the folder are picked up when
+    present.  Returns (density, temperature or None, [vx, vy, vz] or None)."""
+    import os
+    vbx = str(vbx)
+    name = os.path.basename(vbx.rstrip("/\\"))
+    density_file = os.path.join(vbx, f"{name}_mip0.vbx") if num_mips > 1 else vbx
+    density = Volume.load_vbx(density_file, num_mips=num_mips, fp16=fp16, lib=lib)
+    folder = vbx if num_mips > 1 else os.path.dirname(vbx)
+    base = name if num_mips > 1 else os.path.splitext(name)[0]
+    tf = os.path.join(folder, f"{base}_temperature.vbx")
+    temperature = Volume.load_vbx(tf, num_mips=1, fp16=fp16, lib=lib) if os.path.exists(tf) else None
+    vfs = [os.path.join(folder, f"{base}_velocity_{a}.vbx") for a in "xyz"]
+    velocity = [Volume.load_vbx(f, signed=True, lib=lib) for f in vfs] if all(os.path.exists(f) for f in vfs) else None
+    return density, temperature, velocity
 
 
 class VolumetricReSTIR:
