@@ -437,6 +437,35 @@ int vr_selftest_umma(const uint16_t* A, const uint16_t* B, float* D, int32_t var
 /* For n pixel cases (px, py, sampleNumber) returns the first `draws` values of sampleNext1D. */
 int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out);
 
+/* ---- post-process passes around the frame loop (no part of the reference's ReSTIR pass) ----
+ * Accumulation (AccumulatePass, Accumulate.cs.slang:55-125): running per-pixel sums of RGBA32F
+ * frames in double, single or compensated single precision (AccumulatePass.h:66-71);
+ * vr_accumulate adds one frame and, if out_rgba is not NULL, writes the running mean
+ * (float)(sum / count).  vr_accumulator_reset restarts the sums. */
+#define VR_ACCUM_DOUBLE 0
+#define VR_ACCUM_SINGLE 1
+#define VR_ACCUM_SINGLE_COMPENSATED 2
+typedef struct vr_accumulator vr_accumulator;
+int vr_accumulator_create(int32_t width, int32_t height, int32_t precision, vr_accumulator** out);
+void vr_accumulator_destroy(vr_accumulator* acc);
+void vr_accumulator_reset(vr_accumulator* acc);
+int64_t vr_accumulator_count(const vr_accumulator* acc);
+int vr_accumulate(vr_accumulator* acc, const float* frame_rgba_device, float* out_rgba_device, void* stream);
+/* Error against a reference image (ErrorMeasurePass: ErrorMeasurer.cs.slang and the reduction of
+ * ErrorMeasurePass.cpp:216-250): per pixel and channel |src - ref|, squared with
+ * VR_ERRM_SQUARED, (src - ref)^2 / (ref^2 + eps) with VR_ERRM_RELATIVE (relative MSE),
+ * averaged over RGB with VR_ERRM_AVERAGE, zero where world_pos.w == 0 with
+ * VR_ERRM_IGNORE_BACKGROUND; error_out[c] = the channel's sum over pixels / pixel count, summed
+ * in FP64 in a fixed order.  diff_out (optional, device) receives the per-pixel terms.
+ * Synchronises the stream. */
+#define VR_ERRM_IGNORE_BACKGROUND 1
+#define VR_ERRM_SQUARED 2
+#define VR_ERRM_AVERAGE 4
+#define VR_ERRM_RELATIVE 8
+int vr_error_measure(const float* src_rgba_device, const float* ref_rgba_device, const float* world_pos_device_or_null,
+                     int32_t width, int32_t height, int32_t mode, float eps, double error_out[3],
+                     float* diff_out_device_or_null, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,9 @@ def build(force=False, jobs=None):
     obj = BUILD / "noalloc.o"
     src = CSRC / "noalloc.cu"
     units.append((obj, [src, CSRC / "vr_noalloc.h"] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))
+    obj = BUILD / "post.o"
+    src = CSRC / "post.cu"
+    units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))
     obj = BUILD / "context.o"
     src = CSRC / "context.cu"
     units.append((obj, [src] + hdrs, [nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)]))

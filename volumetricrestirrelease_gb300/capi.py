@@ -137,6 +137,12 @@ SIGNATURES = {
     "vr_volume_load_vbx": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(_P)]),
     "vr_volume_save_vbx": (_i32, [_P, C.c_char_p]),
     "vr_volume_vbx_error": (C.c_char_p, []),
+    "vr_accumulator_create": (_i32, [_i32, _i32, _i32, C.POINTER(_P)]),
+    "vr_accumulator_destroy": (None, [_P]),
+    "vr_accumulator_reset": (None, [_P]),
+    "vr_accumulator_count": (C.c_int64, [_P]),
+    "vr_accumulate": (_i32, [_P, _P, _P, _P]),
+    "vr_error_measure": (_i32, [_P, _P, _P, _i32, _i32, _i32, _f32, C.POINTER(C.c_double), _P, _P]),
     "vr_animation_frame": (_i32, [_P]),
     "vr_batch_create": (_i32, [C.POINTER(_P), _i32, C.POINTER(_P)]),
     "vr_batch_destroy": (None, [_P]),
