@@ -413,10 +413,16 @@ struct HDDA {
         tSide = ((fl - pFlt + mk3(0.5f)) * mk3((float)pStep[0], (float)pStep[1], (float)pStep[2]) + mk3(0.5f)) * tDel + mk3(t.x);
         p[0] = f2i(fl.x); p[1] = f2i(fl.y); p[2] = f2i(fl.z);
     }
+    // Next (gvdbDda.slang:140-149).  Deviation: when the three side distances are equal (the ray
+    // passes through a cell corner) the reference sets no mask, so Step does not move: the node
+    // walk then creeps on by epsilon and re-enters the brick, and the voxel walk inside a brick
+    // repeats a zero-length step until its step limit, dropping the rest of that brick.  Here
+    // the z axis steps, as it does for the tie z == y < x.
     void Next() {
         mask[0] = (tSide.x < tSide.y) & (tSide.x <= tSide.z);
         mask[1] = (tSide.y < tSide.z) & (tSide.y <= tSide.x);
         mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
+        if (!(mask[0] | mask[1] | mask[2]) && tSide.x == tSide.z) mask[2] = 1;
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
     // Step (gvdbDda.slang:151-156) advances the masked axes by tDel.  The reference writes

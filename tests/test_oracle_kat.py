@@ -137,3 +137,30 @@ def test_segment_ending_before_the_next_brick(vlib, method, linear):
             assert 0.0 <= t <= 1.0 + 1e-6, t
     # about 6.7 voxels of density 0.5 (sigma_t 3, voxel 1/64) lie on the segment
     assert np.mean(ts) == pytest.approx(math.exp(-SIGMA_T * 0.5 * (16 - 9.3) / 64 / d[0]), rel=0.15)
+
+
+@pytest.mark.parametrize("method,linear", [(capi.VR_TRACK_ANALYTIC, 0), (capi.VR_TRACK_RAY_MARCHING, 0)])
+def test_ray_through_cell_corners(vlib, method, linear):
+    """A ray along the cube diagonal from a lattice point crosses every cell at a corner, where
+    the three side distances of the DDA tie.  The reference's DDA then sets no step mask and
+    stalls: the brick walk drops the rest of each brick (here T came out near 1).  The whole
+    chord must count, and a ray a hair off the lattice must agree."""
+    from oracle.oracle import Oracle
+    g = np.zeros((64, 64, 64), np.float32)
+    g[16:48, 16:48, 16:48] = 0.5
+    vol = Volume.dense(g, (0.0, 0.0, 0.0), 1.0 / 64, num_mips=1, lib=vlib)
+    m = capi.Medium()
+    m.sigma_s[:] = [SIGMA_T * 0.8] * 3
+    m.sigma_a[:] = [SIGMA_T - SIGMA_T * 0.8] * 3
+    m.g = 0.0
+    m.density_scale = 1.0
+    o = Oracle(8, 8, capi.default_options(vlib))
+    o.set_volume(vol, m)
+    d = (1.0 / math.sqrt(3.0),) * 3
+    expect = math.exp(-SIGMA_T * 0.5 * (32 / 64) * math.sqrt(3.0))
+    on = _tr(o, (8 / 64,) * 3, d, 1e30, method, linear=linear)
+    off = _tr(o, (8.0013 / 64, 7.9991 / 64, 8.0007 / 64), d, 1e30, method, linear=linear)
+    # ray marching is a fixed-step quadrature: within a few percent of the closed form
+    tol = 0.05 if method == capi.VR_TRACK_RAY_MARCHING else 2e-3
+    assert on == pytest.approx(expect, rel=tol)
+    assert on == pytest.approx(off, rel=0.01 if method == capi.VR_TRACK_RAY_MARCHING else 2e-3)

@@ -405,10 +405,13 @@ struct HDDA {
         tDel = mk3(vr::fabs_(1.0f / dir.x), vr::fabs_(1.0f / dir.y), vr::fabs_(1.0f / dir.z));
         finishPrepare(pos + dir * t.x - vmin);
     }
+    // a three-way tie (the ray through a cell corner) steps the z axis; the reference sets no
+    // mask there and stalls the walk (see the oracle's HDDA::Next)
     __device__ __forceinline__ void next() {
         mask[0] = (tSide.x < tSide.y) & (tSide.x <= tSide.z);
         mask[1] = (tSide.y < tSide.z) & (tSide.y <= tSide.x);
         mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
+        if (!(mask[0] | mask[1] | mask[2]) && tSide.x == tSide.z) mask[2] = 1;
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
     // advances only the masked axes (a zero direction component has tDel = inf)
