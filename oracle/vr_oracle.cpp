@@ -417,12 +417,13 @@ struct HDDA {
     // passes through a cell corner) the reference sets no mask, so Step does not move: the node
     // walk then creeps on by epsilon and re-enters the brick, and the voxel walk inside a brick
     // repeats a zero-length step until its step limit, dropping the rest of that brick.  Here
-    // the z axis steps, as it does for the tie z == y < x.
+    // the z axis steps, as it does for the tie z == y < x.  Without NaN side distances (a zero
+    // direction component gives an infinite one), z is the reference's choice exactly when
+    // neither x nor y is, apart from that tie.
     void Next() {
         mask[0] = (tSide.x < tSide.y) & (tSide.x <= tSide.z);
         mask[1] = (tSide.y < tSide.z) & (tSide.y <= tSide.x);
-        mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
-        if (!(mask[0] | mask[1] | mask[2]) && tSide.x == tSide.z) mask[2] = 1;
+        mask[2] = !(mask[0] | mask[1]);       // (z < x) & (z <= y) in the reference, or the tie
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
     // Step (gvdbDda.slang:151-156) advances the masked axes by tDel.  The reference writes

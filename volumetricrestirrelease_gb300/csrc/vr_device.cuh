@@ -410,8 +410,7 @@ struct HDDA {
     __device__ __forceinline__ void next() {
         mask[0] = (tSide.x < tSide.y) & (tSide.x <= tSide.z);
         mask[1] = (tSide.y < tSide.z) & (tSide.y <= tSide.x);
-        mask[2] = (tSide.z < tSide.x) & (tSide.z <= tSide.y);
-        if (!(mask[0] | mask[1] | mask[2]) && tSide.x == tSide.z) mask[2] = 1;
+        mask[2] = !(mask[0] | mask[1]);       // (z < x) & (z <= y), or the three-way tie
         t.y = mask[0] ? tSide.x : (mask[1] ? tSide.y : tSide.z);
     }
     // advances only the masked axes (a zero direction component has tDel = inf)
