@@ -313,6 +313,14 @@ int vr_render_frame(vr_context* ctx, const vr_camera* cam, float* out_rgba_devic
 /* Same frame, host output buffer: copies the image back (synchronises the stream). */
 int vr_render_frame_host(vr_context* ctx, const vr_camera* cam, float* out_rgba_host,
                          void* stream);
+/* Pipelined host output: renders into one of two device staging images and copies it to
+ * out_rgba_host on the context's copy stream without waiting, so frame n's copy overlaps frame
+ * n+1's kernels (use pinned host memory for a real overlap).  At most two frames are in flight:
+ * a call first waits for the copy issued two calls earlier.  out_rgba_host may be read after
+ * vr_host_frames_wait, or once the second call after its own has returned.  Bounded-loop errors
+ * of the device are reported by vr_host_frames_wait. */
+int vr_render_frame_host_async(vr_context* ctx, const vr_camera* cam, float* out_rgba_host, void* stream);
+int vr_host_frames_wait(vr_context* ctx);
 
 /* ---- allocation-free frame (no counterpart in the reference) ----
  * Renders one frame without temporal history into out_rgba_device, keeping every per-pixel

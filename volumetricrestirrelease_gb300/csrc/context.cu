@@ -261,6 +261,13 @@ struct vr_context {
     // default stream), forked after select and joined at the end of the frame
     cudaStream_t side = nullptr;
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    // pipelined host output: two device staging images, their copies on a copy stream
+    float* hostStage[2] = {nullptr, nullptr};
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t copyDone[2] = {nullptr, nullptr}, rendered[2] = {nullptr, nullptr};
+    bool copyPending[2] = {false, false};
+    int hostIdx = 0;
+    size_t hostStageBytes = 0;
     // learned target: network (FP32 master weights, Adam moments, BF16 copy) and the buffers
     // of the split initial pass
     float *netW = nullptr, *netM = nullptr, *netV = nullptr, *netG = nullptr, *netBias = nullptr;
@@ -729,6 +736,12 @@ void vr_destroy(vr_context* c) {
     if (c->side) cudaStreamDestroy(c->side);
     if (c->evFork) cudaEventDestroy(c->evFork);
     if (c->evJoin) cudaEventDestroy(c->evJoin);
+    for (int i = 0; i < 2; ++i) {
+        if (c->copyDone[i]) { cudaEventSynchronize(c->copyDone[i]); cudaEventDestroy(c->copyDone[i]); }
+        if (c->rendered[i]) cudaEventDestroy(c->rendered[i]);
+        cudaFree(c->hostStage[i]);
+    }
+    if (c->copyStream) cudaStreamDestroy(c->copyStream);
     delete c;
 }
 
@@ -1169,6 +1182,66 @@ int vr_render_frame(vr_context* c, const vr_camera* cam, float* out_rgba, float*
     c->prev = cf;
     c->frameCount++;
     return VR_OK;
+}
+
+static int read_status(vr_context* c) {
+    int status = 0;
+    cudaMemcpy(&status, c->status, 4, cudaMemcpyDeviceToHost);
+    if (status) {
+        int zero = 0;
+        cudaMemcpy(c->status, &zero, 4, cudaMemcpyHostToDevice);
+        c->err = "a bounded device loop hit its iteration limit";
+        return VR_ERR_LOOP_LIMIT;
+    }
+    return VR_OK;
+}
+
+int vr_render_frame_host_async(vr_context* c, const vr_camera* cam, float* out_rgba_host, void* stream) {
+    if (!c || !out_rgba_host) return VR_ERR_INVALID_ARG;
+    const size_t bytes = (size_t)c->W * c->H * 16;
+    if (!c->copyStream) {
+        if (cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess) return check_cuda(c, "copy stream");
+        for (int i = 0; i < 2; ++i) {
+            cudaEventCreateWithFlags(&c->copyDone[i], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&c->rendered[i], cudaEventDisableTiming);
+        }
+    }
+    const int i = c->hostIdx;
+    if (c->copyPending[i]) {                       // the copy issued two calls ago
+        if (cudaEventSynchronize(c->copyDone[i]) != cudaSuccess) return check_cuda(c, "host copy");
+        c->copyPending[i] = false;
+    }
+    if (!c->hostStage[i] || c->hostStageBytes != bytes) {
+        for (int k = 0; k < 2; ++k) {
+            if (c->copyPending[k]) { cudaEventSynchronize(c->copyDone[k]); c->copyPending[k] = false; }
+            cudaFree(c->hostStage[k]);
+            c->hostStage[k] = nullptr;
+        }
+        for (int k = 0; k < 2; ++k)
+            if (cudaMalloc(&c->hostStage[k], bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
+        c->hostStageBytes = bytes;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int r = vr_render_frame(c, cam, c->hostStage[i], nullptr, stream);
+    if (r) return r;
+    cudaEventRecord(c->rendered[i], st);
+    cudaStreamWaitEvent(c->copyStream, c->rendered[i], 0);
+    cudaMemcpyAsync(out_rgba_host, c->hostStage[i], bytes, cudaMemcpyDeviceToHost, c->copyStream);
+    cudaEventRecord(c->copyDone[i], c->copyStream);
+    c->copyPending[i] = true;
+    c->d2h = (int64_t)bytes;
+    c->hostIdx ^= 1;
+    return check_cuda(c, "host copy");
+}
+
+int vr_host_frames_wait(vr_context* c) {
+    if (!c) return VR_ERR_INVALID_ARG;
+    for (int i = 0; i < 2; ++i)
+        if (c->copyPending[i]) {
+            if (cudaEventSynchronize(c->copyDone[i]) != cudaSuccess) return check_cuda(c, "host copy");
+            c->copyPending[i] = false;
+        }
+    return read_status(c);
 }
 
 int vr_render_frame_host(vr_context* c, const vr_camera* cam, float* out_rgba_host, void* stream) {
