@@ -577,24 +577,27 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * args.steps / (ms / 1000.0)
-    queries = len(rd.export_learned(1)) if rank == 0 else 0
-    net_params, net_box = rd.net_params(), rd.net_box()
     stage_names = ["initial_stage", "spatial_final", "training", "k_lp_generate", "k_net_infer", "k_lp_select"]
     kernel_ms = dict(zip(stage_names, kms))
 
-    # ---- learned form, end to end through the pipelined host entry point: each frame's image
-    # lands in one of two pinned host buffers while the next frame renders; the timed region
-    # ends when the last image is in host memory ----
+    # ---- learned form, end to end through the pipelined host entry point, on the same frames
+    # (a fresh context, the same warm-up): each frame's image lands in one of two pinned host
+    # buffers while the next frame renders; the timed region ends when the last image is in
+    # host memory ----
+    queries = len(rd.export_learned(1)) if rank == 0 else 0
+    net_params, net_box = rd.net_params(), rd.net_box()
+    del rd
+    rd = VolumetricReSTIR(W, H, opts.as_dict(), lib=lib)
+    rd.setScene(vols[True], sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
     pinned = [torch.empty((H, W, 4), dtype=torch.float32).pin_memory() for _ in range(2)]
     hptr = [C.cast(C.c_void_p(p.data_ptr()), C.POINTER(C.c_float)) for p in pinned]
-    n0 = args.warmup + args.steps
-    for f in range(n0, n0 + 2):
+    for f in range(args.warmup):
         assert lib.vr_render_frame_host_async(rd._h, C.byref(sc.camera(f)), hptr[f % 2], C.c_void_p(sptr)) == 0
     assert lib.vr_host_frames_wait(rd._h) == 0
     barrier()
     torch.cuda.synchronize()
     t = time.perf_counter()
-    for f in range(n0 + 2, n0 + 2 + args.steps):
+    for f in range(args.warmup, args.warmup + args.steps):
         r = lib.vr_render_frame_host_async(rd._h, C.byref(sc.camera(f)), hptr[f % 2], C.c_void_p(sptr))
         assert r == 0, r
     assert lib.vr_host_frames_wait(rd._h) == 0
