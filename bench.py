@@ -118,6 +118,22 @@ def _dist():
     return ws, rank
 
 
+def max_over_ranks(x, ws, device="cuda"):
+    """The largest of every rank's x (the slowest replica's time); x itself when ws == 1."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(ws, steps, ms):
+    """Frames per second of the whole job: every rank renders `steps` frames of its replica in
+    the slowest rank's `ms` milliseconds."""
+    return ws * steps / (ms / 1000.0)
+
+
 def _scene(args, fp16=False, static=False, width=None, height=None):
     from volumetricrestirrelease_gb300 import scenes
     sc = scenes.full(width=width or args.width, height=height or args.height, fp16=fp16)
@@ -572,11 +588,8 @@ def run_gpu(args):
     rd = VolumetricReSTIR(W, H, opts.as_dict(), lib=lib)
     rd.setScene(vols[True], sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
     ms, kms, launches, clocks = _time_frames(rd, sc, out, sptr, args.warmup, args.steps, clock_index=local, barrier=barrier)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.steps / (ms / 1000.0)
+    ms = max_over_ranks(ms, ws)
+    value = whole_job_rate(ws, args.steps, ms)
     stage_names = ["initial_stage", "spatial_final", "training", "k_lp_generate", "k_net_infer", "k_lp_select"]
     kernel_ms = dict(zip(stage_names, kms))
 
@@ -604,7 +617,7 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t
     h2d, d2h = C.c_int64(), C.c_int64()
     lib.vr_last_transfer_bytes(rd._h, C.byref(h2d), C.byref(d2h))
-    e2e = ws * args.steps / e2e_s
+    e2e = whole_job_rate(ws, args.steps, max_over_ranks(e2e_s * 1000.0, ws))
     del rd
 
     # ---- plain form (FP32 bricks, M=32), same frames ----
@@ -613,7 +626,7 @@ def run_gpu(args):
     rp = VolumetricReSTIR(W, H, optp.as_dict(), lib=lib)
     rp.setScene(vols[False], scp.medium, scp.lights, scp.env_rgb, scp.env_scale)
     msp, kmsp, _, _ = _time_frames(rp, scp, out, sptr, args.warmup, args.steps, barrier=barrier)
-    plain_fps = ws * args.steps / (msp / 1000.0)
+    plain_fps = whole_job_rate(ws, args.steps, max_over_ranks(msp, ws))
     del rp
 
     batched = None
