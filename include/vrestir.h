@@ -445,6 +445,12 @@ int vr_selftest_umma(const uint16_t* A, const uint16_t* B, float* D, int32_t var
 /* For n pixel cases (px, py, sampleNumber) returns the first `draws` values of sampleNext1D. */
 int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out);
 
+/* ---- fault injection on the host (testing) ----
+ * The n-th device allocation that any context makes from now on (n = 0: the next one) fails as
+ * if the device were out of memory; the calls then return VR_ERR_OOM and leave the context
+ * usable.  n < 0 switches the injection off. */
+void vr_debug_fail_allocation(int32_t n);
+
 /* ---- post-process passes around the frame loop (no part of the reference's ReSTIR pass) ----
  * Accumulation (AccumulatePass, Accumulate.cs.slang:55-125): running per-pixel sums of RGBA32F
  * frames in double, single or compensated single precision (AccumulatePass.h:66-71);

@@ -135,6 +135,7 @@ SIGNATURES = {
     "vr_set_animation": (_i32, [_P, C.POINTER(_P), _i32, C.POINTER(_P), C.POINTER(_P), _f32]),
     "vr_render_frame_host_async": (_i32, [_P, C.POINTER(Camera), C.POINTER(_f32), _P]),
     "vr_host_frames_wait": (_i32, [_P]),
+    "vr_debug_fail_allocation": (None, [_i32]),
     "vr_volume_create_dense_signed": (_i32, [_P, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
     "vr_volume_load_vbx": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(_P)]),
     "vr_volume_save_vbx": (_i32, [_P, C.c_char_p]),

@@ -193,11 +193,27 @@ void build_importance(HostEnv& e) {
     }
 }
 
+}  // namespace
+
+// Every device allocation of the library's contexts goes through dev_malloc, so that host-side
+// fault injection (vr_debug_fail_allocation) can make the n-th one fail as an out-of-memory would.
+static std::atomic<int64_t> g_failAlloc{-1};
+template <class T>
+static cudaError_t dev_malloc(T** p, size_t bytes) {
+    if (g_failAlloc.load() >= 0 && g_failAlloc.fetch_sub(1) == 0) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc((void**)p, bytes);
+}
+
+namespace {
+
 template <class T>
 T* dalloc(size_t n) {
     T* p = nullptr;
     if (n == 0) n = 1;
-    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+    if (dev_malloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
     return p;
 }
 
@@ -364,6 +380,10 @@ static int net_alloc(vr_context* c, int partRows) {
         c->netG = dalloc<float>(lpn::kParamsPad); c->netBias = dalloc<float>(320); c->netWbf = dalloc<uint16_t>(5 * 4096);
         c->netScalar = dalloc<float>(4);
         if (!c->netW || !c->netM || !c->netV || !c->netG || !c->netBias || !c->netWbf || !c->netScalar) {
+            cudaFree(c->netW); cudaFree(c->netM); cudaFree(c->netV); cudaFree(c->netG); cudaFree(c->netBias); cudaFree(c->netWbf);
+            cudaFree(c->netScalar);
+            c->netW = c->netM = c->netV = c->netG = c->netBias = c->netScalar = nullptr;
+            c->netWbf = nullptr;
             c->err = "out of device memory (network)"; return VR_ERR_OOM;
         }
         if (vrk::net_setup() != cudaSuccess) { c->err = "network kernel setup failed"; return VR_ERR_CUDA; }
@@ -374,7 +394,11 @@ static int net_alloc(vr_context* c, int partRows) {
         cudaFree(c->netPart); cudaFree(c->netLossPart);
         c->netPart = dalloc<float>((size_t)partRows * lpn::kParamsPad);
         c->netLossPart = dalloc<float>(partRows);
-        if (!c->netPart || !c->netLossPart) { c->netPartRows = 0; c->err = "out of device memory (network gradients)"; return VR_ERR_OOM; }
+        if (!c->netPart || !c->netLossPart) {
+            cudaFree(c->netPart); cudaFree(c->netLossPart);
+            c->netPart = c->netLossPart = nullptr;
+            c->netPartRows = 0; c->err = "out of device memory (network gradients)"; return VR_ERR_OOM;
+        }
         c->netPartRows = partRows;
     }
     return VR_OK;
@@ -713,7 +737,7 @@ vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int
     c->opts = *opts;
     c->W = width; c->H = height;
     for (auto& e : c->ev) cudaEventCreate(&e);
-    if (cudaMalloc(&c->status, sizeof(int)) != cudaSuccess) { delete c; if (err) *err = VR_ERR_OOM; return nullptr; }
+    if (dev_malloc(&c->status, sizeof(int)) != cudaSuccess) { delete c; if (err) *err = VR_ERR_OOM; return nullptr; }
     cudaMemset(c->status, 0, sizeof(int));
     c->scene.status = c->status;
     if (err) *err = VR_OK;
@@ -809,7 +833,7 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
     if (!g.valid) { c->err = "temperature volume has no mip 0"; return VR_ERR_INVALID_ARG; }
     auto up = [&](const void* src, size_t bytes) -> void* {
         void* p = nullptr;
-        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        if (dev_malloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
         c->emisAllocs.push_back(p);
         if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
         return p;
@@ -828,7 +852,12 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
     d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
     if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
     else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
-    if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) { c->err = "out of device memory (temperature)"; return VR_ERR_OOM; }
+    if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) {
+        for (void* q : c->emisAllocs) cudaFree(q);
+        c->emisAllocs.clear();
+        memset(&c->scene.tslot, 0, sizeof(c->scene.tslot));
+        c->err = "out of device memory (temperature)"; return VR_ERR_OOM;
+    }
     float tab[384];
     if (lut) memcpy(tab, lut, sizeof(tab));
     else vr::blackbody_lut(tab);
@@ -861,7 +890,7 @@ int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
         if (!g.valid) continue;
         auto up = [&](const void* src, size_t bytes) -> void* {
             void* p = nullptr;
-            if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+            if (dev_malloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
             c->sceneAllocs.push_back(p);
             if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
             return p;
@@ -878,7 +907,13 @@ int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
         d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
         if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
         else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
-        if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) { c->err = "out of device memory (volume)"; return VR_ERR_OOM; }
+        if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) {
+            for (void* q : c->sceneAllocs) cudaFree(q);
+            c->sceneAllocs.clear();
+            memset(c->scene.slots, 0, sizeof(vrd::DevSlot) * VR_NUM_SLOTS);
+            c->hasVolume = false;
+            c->err = "out of device memory (volume)"; return VR_ERR_OOM;
+        }
     }
     c->scene.sigma_s = mk3(m->sigma_s[0], m->sigma_s[1], m->sigma_s[2]);
     c->scene.sigma_a = mk3(m->sigma_a[0], m->sigma_a[1], m->sigma_a[2]);
@@ -906,7 +941,7 @@ static bool upload_grid(const vr::GridSlot& g, vrd::DevSlot& d, std::vector<void
     if (!g.valid) return true;
     auto up = [&](const void* src, size_t bytes) -> void* {
         void* p = nullptr;
-        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        if (dev_malloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
         allocs.push_back(p);
         if (bytes) cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
         return p;
@@ -1027,6 +1062,8 @@ int vr_set_animation(vr_context* c, const vr_volume* const* frames, int32_t n, c
 
 int32_t vr_animation_frame(const vr_context* c) { return c ? c->animId : -1; }
 
+void vr_debug_fail_allocation(int32_t n) { g_failAlloc.store(n < 0 ? -1 : (int64_t)n); }
+
 int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const vr_env_map* env) {
     if (!c || n < 0 || n > vrd::kMaxLights || (n > 0 && !lights)) { if (c) c->err = "at most 64 point lights"; return VR_ERR_INVALID_ARG; }
     c->scene.numLights = n;
@@ -1034,7 +1071,9 @@ int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const 
         for (int k = 0; k < 3; ++k) { c->scene.lightPos[i][k] = lights[i].pos[k]; c->scene.lightI[i][k] = lights[i].intensity[k]; }
     for (void* p : c->envAllocs) cudaFree(p);
     c->envAllocs.clear();
-    c->scene.hasEnv = env != nullptr;
+    c->scene.hasEnv = 0;
+    c->scene.envRGB = nullptr;
+    c->scene.imp = nullptr;
     if (env) {
         if (!env->rgb || env->width <= 0 || env->height <= 0) { c->err = "invalid environment map"; return VR_ERR_INVALID_ARG; }
         HostEnv& e = c->env;
@@ -1042,7 +1081,11 @@ int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const 
         e.rgb.assign(env->rgb, env->rgb + (size_t)e.w * e.h * 3);
         build_importance(e);
         float *drgb = nullptr, *dimp = nullptr;
-        if (cudaMalloc(&drgb, e.rgb.size() * 4) != cudaSuccess || cudaMalloc(&dimp, e.imp.size() * 4) != cudaSuccess) { c->err = "out of device memory (env)"; return VR_ERR_OOM; }
+        if (dev_malloc(&drgb, e.rgb.size() * 4) != cudaSuccess || dev_malloc(&dimp, e.imp.size() * 4) != cudaSuccess) {
+            cudaFree(drgb); cudaFree(dimp);
+            c->optionsChanged = true;
+            c->err = "out of device memory (env)"; return VR_ERR_OOM;
+        }
         c->envAllocs.push_back(drgb); c->envAllocs.push_back(dimp);
         cudaMemcpy(drgb, e.rgb.data(), e.rgb.size() * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dimp, e.imp.data(), e.imp.size() * 4, cudaMemcpyHostToDevice);
@@ -1055,6 +1098,7 @@ int vr_set_lights(vr_context* c, const vr_point_light* lights, int32_t n, const 
         memcpy(c->scene.impOff, e.off, sizeof(e.off));
         c->scene.impDim = 512;
         c->scene.impBaseMip = 9;
+        c->scene.hasEnv = 1;
     }
     c->optionsChanged = true;
     return VR_OK;
@@ -1218,7 +1262,7 @@ int vr_render_frame_host_async(vr_context* c, const vr_camera* cam, float* out_r
             c->hostStage[k] = nullptr;
         }
         for (int k = 0; k < 2; ++k)
-            if (cudaMalloc(&c->hostStage[k], bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
+            if (dev_malloc(&c->hostStage[k], bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
         c->hostStageBytes = bytes;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -1252,7 +1296,7 @@ int vr_render_frame_host(vr_context* c, const vr_camera* cam, float* out_rgba_ho
     static thread_local std::vector<std::pair<size_t, float*>> scratch;
     for (auto& s : scratch) if (s.first == bytes) d = s.second;
     if (!d) {
-        if (cudaMalloc(&d, bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
+        if (dev_malloc(&d, bytes) != cudaSuccess) { c->err = "out of device memory (output)"; return VR_ERR_OOM; }
         scratch.push_back({bytes, d});
     }
     int r = vr_render_frame(c, cam, d, nullptr, stream);
@@ -1723,10 +1767,10 @@ __global__ void k_selftest_rng(const uint32_t* cases, int n, int draws, float* o
 extern "C" int vr_selftest_math(int32_t op, const float* a, const float* b, float* out, int32_t n) {
     if (!a || !out || n <= 0 || op < 0 || op > 7) return VR_ERR_INVALID_ARG;
     float *da, *db = nullptr, *dout;
-    if (cudaMalloc(&da, n * 4) != cudaSuccess) return VR_ERR_CUDA;
-    cudaMalloc(&dout, n * 4);
+    if (dev_malloc(&da, n * 4) != cudaSuccess) return VR_ERR_CUDA;
+    dev_malloc(&dout, n * 4);
     cudaMemcpy(da, a, n * 4, cudaMemcpyHostToDevice);
-    if (b) { cudaMalloc(&db, n * 4); cudaMemcpy(db, b, n * 4, cudaMemcpyHostToDevice); }
+    if (b) { dev_malloc(&db, n * 4); cudaMemcpy(db, b, n * 4, cudaMemcpyHostToDevice); }
     k_selftest_math<<<(n + 255) / 256, 256>>>(op, da, db, dout, n);
     cudaMemcpy(out, dout, n * 4, cudaMemcpyDeviceToHost);
     cudaFree(da); cudaFree(db); cudaFree(dout);
@@ -1735,8 +1779,8 @@ extern "C" int vr_selftest_math(int32_t op, const float* a, const float* b, floa
 extern "C" int vr_selftest_rng(const uint32_t* cases, int32_t n, int32_t draws, float* out) {
     if (!cases || !out || n <= 0 || draws <= 0) return VR_ERR_INVALID_ARG;
     uint32_t* dc; float* dout;
-    if (cudaMalloc(&dc, (size_t)n * 12) != cudaSuccess) return VR_ERR_CUDA;
-    cudaMalloc(&dout, (size_t)n * draws * 4);
+    if (dev_malloc(&dc, (size_t)n * 12) != cudaSuccess) return VR_ERR_CUDA;
+    dev_malloc(&dout, (size_t)n * draws * 4);
     cudaMemcpy(dc, cases, (size_t)n * 12, cudaMemcpyHostToDevice);
     k_selftest_rng<<<(n + 127) / 128, 128>>>(dc, n, draws, dout);
     cudaMemcpy(out, dout, (size_t)n * draws * 4, cudaMemcpyDeviceToHost);
@@ -1964,7 +2008,7 @@ static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs,
         cudaFree(b->dData);
         cudaFreeHost(b->hStage);
         b->dData = nullptr; b->hStage = nullptr; b->dataBytes = 0;
-        if (cudaMalloc(&b->dData, need) != cudaSuccess || cudaMallocHost(&b->hStage, need) != cudaSuccess) {
+        if (dev_malloc(&b->dData, need) != cudaSuccess || cudaMallocHost(&b->hStage, need) != cudaSuccess) {
             b->err = "out of memory (batch descriptors)";
             return VR_ERR_OOM;
         }
