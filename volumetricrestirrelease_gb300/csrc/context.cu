@@ -19,6 +19,15 @@
 
 #include "../../include/vrestir.h"
 #include "lp_net.h"
+// NVTX ranges around the passes of a frame (header-only NVTX 3: no cost unless a profiler attaches)
+#if !defined(VR_HOST_EMULATION)
+#include <nvtx3/nvToolsExt.h>
+#define VR_RANGE(name) nvtxRangePushA(name)
+#define VR_RANGE_END() nvtxRangePop()
+#else
+#define VR_RANGE(name) ((void)0)
+#define VR_RANGE_END() ((void)0)
+#endif
 #include "vr_kernels.cuh"
 #include "vr_lp.h"
 #include "vr_volume.h"
@@ -1651,11 +1660,17 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     const bool lpOn = lp_active(c);
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+        VR_RANGE("vr.generate");
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
+        VR_RANGE_END();
         rec();
+        VR_RANGE("vr.infer");
         vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
+        VR_RANGE_END();
         rec();
+        VR_RANGE("vr.select");
         launch_lp_select<MB>(P, B, c->lp, grid, block, st);
+        VR_RANGE_END();
         c->launches += 3;
         c->lpFrameDone = true;
         // online training of the network on this frame's own queries (used from the next frame
@@ -1673,7 +1688,9 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             c->lp.targetMethod = o.mLearnedTargetMethod;
             launch_lp_train_gen<MB>(P, c->lp, lp_train_seed(o.mLearnedSeed, c->frameCount), c->side);
             c->launches++;
+            VR_RANGE("vr.train");
             lp_train_steps(c, c->lp.train, o.mLearnedTrainSamples, c->side);
+            VR_RANGE_END();
             trainEv[1] = take_event(c);
             cudaEventRecord(trainEv[1], c->side);
             cudaEventRecord(c->evJoin, c->side);
@@ -1681,7 +1698,9 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             c->lastSteps = 0;
         }
     } else {
+        VR_RANGE("vr.initial");
         launch_initial<MB>(P, B, grid, block, st);
+        VR_RANGE_END();
         c->launches++;
     }
     mark();
@@ -1710,13 +1729,17 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             S.writeHistory = temporal;
             int r2 = ((o.mSpatialReuseRounds + 1) * c->frameCount + r) % 16;
             neighbor_offsets(o, r2, S.offs);
+            VR_RANGE("vr.spatial");
             launch_spatial<MB>(P, B, S, grid, block, st);
+            VR_RANGE_END();
             c->launches++;
             totalRoundId++;
             if (S.last) mark();
         }
     } else {
+        VR_RANGE("vr.final");
         launch_final<MB>(P, B, 0, grid, block, st);
+        VR_RANGE_END();
         c->launches++;
         mark();
     }
