@@ -325,7 +325,7 @@ __device__ inline int findBrick(const DevSlot& s, f3 pos, f3& vmin) {
     vmin = nodeVmin(s, 0, br);
     return br;
 }
-static __device__ __noinline__ float densityWorld(f3 pw, int mip) {
+static __device__ __forceinline__ float densityWorld(f3 pw, int mip) {
     const DevSlot& s = c_scene.slots[mip];
     f3 p = mulPoint(pw, s.M);
     if (p.x < 0.f || p.y < 0.f || p.z < 0.f || p.x >= s.bmaxf || p.y >= s.bmaxf || p.z >= s.bmaxf) return 0.f;
@@ -835,7 +835,7 @@ __device__ inline float trResidual(const Ray& r, int mip, vr::Rng& sg, bool anal
     trackVolume(r, mip, sg, a, false);
     return a.Tr;
 }
-static __device__ __noinline__ float computeVisibility(const Ray& ray, vr::Rng& sg, int samples, int mip, bool lin, uint32_t method, float tss) {
+static __device__ __forceinline__ float computeVisibility(const Ray& ray, vr::Rng& sg, int samples, int mip, bool lin, uint32_t method, float tss) {
     float vis = 0;
     for (int i = 0; i < samples; i++) {
         if (method == VR_TRACK_RATIO || method == VR_TRACK_RESIDUAL_RATIO || method == VR_TRACK_ANALOG_RESIDUAL_RATIO)
