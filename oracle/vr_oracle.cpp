@@ -1438,9 +1438,12 @@ struct LpVertex { float a, b, uv0, uv1; int lightID, sampledPixel, flags; float 
 const int kLpValid = 1, kLpNeedsT = 2;
 
 // ComputeInitialSample with the shadow ray of the next-event estimate deferred to the network
-// and every resampling uniform drawn up front (the random stream does not depend on T)
-static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf, float preTr, Rng& sg, LpVertex* rec, f3* extra,
-                                    float* queries /* [maxBounces][8] */) {
+// and every resampling uniform drawn up front (the random stream does not depend on T).  The
+// first vertex draws from the pixel's stream; the indirect vertices (bounces >= 1) draw from the
+// candidate's own stream, seeded by (pixel, frame, candidate), so that they can be generated as
+// queued work apart from the other candidates.
+static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf, float preTr, Rng& sgPixel, LpVertex* rec, f3* extra,
+                                    float* queries /* [maxBounces][8] */, int px, int py, int frame, int cid) {
     const Scene& sc = *c.sc;
     const SamplingOptions& options = c.initial;
     const int maxBounces = c.maxBounces;
@@ -1449,7 +1452,11 @@ static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf,
     const f3 sigma_s = sc.med.sigma_s, sigma_a = sc.med.sigma_a;
     const float sigma_t = sc.med.sigma_t;
     int bounce = 0;
+    Rng candidate{};
     for (; bounce < maxBounces; bounce++) {
+        if (bounce == 1)
+            candidate = rng_create((uint32_t)px, (uint32_t)py, 0x40000000u | (((uint32_t)frame * 4096u + (uint32_t)cid) & 0x3FFFFFFFu));
+        Rng& sg = bounce == 0 ? sgPixel : candidate;
         Reservoir out = createNewReservoir();
         out.M = 1;
         float curHitDist, pdfDist = 0, Tr;
@@ -1951,7 +1958,7 @@ struct Oracle {
                     SampleMediumAnalyticGeneric(sc, ray, sg, c.initial.visibilityUseLinearSampler, hd, c.initial.visibilityMipLevel, pd, trs, rs);
                     for (int sid = 0; sid < rs; sid++, cid++) {
                         float depth = ComputeInitialSampleLP(cl, ray, hd[sid], pd[sid], trs[sid], sg, &rec[(size_t)cid * mb],
-                                                             &ex[(size_t)cid * std::max(mb - 1, 1)], q.data());
+                                                             &ex[(size_t)cid * std::max(mb - 1, 1)], q.data(), x, y, frameCount, cid);
                         crec[cid * 2] = depth;
                         crec[cid * 2 + 1] = next1D(sg);
                         int nv = 0;

@@ -42,7 +42,8 @@ namespace vrk {
     void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);        \
     void launch_lp_generate_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
     void launch_lp_select_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
-    void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);
+    void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);          \
+    void launch_lp_bounce_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, int, int, cudaStream_t);
 VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 #undef VR_DECL
 // the network kernels (lp.cu)
@@ -352,6 +353,7 @@ static int alloc_buffers(vr_context* c) {
 static void free_lp(vr_context* c) {
     cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.ex); cudaFree(c->lp.T);
     cudaFree(c->lp.query); cudaFree(c->lp.qlist); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
+    cudaFree(c->lp.paths[0]); cudaFree(c->lp.paths[1]); cudaFree(c->lp.pcount);
     c->lp = vrd::LpBuffers{};
     c->lpSlots = 0; c->lpM = 0; c->lpMB = 0;
 }
@@ -470,14 +472,23 @@ static int lp_alloc(vr_context* c) {
         c->lp.qcount = dalloc<int>(1);
         c->lp.rng = dalloc<uint4>(N);
         c->lp.train = dalloc<float4>(2 * (size_t)std::max(S, 1));
-        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train) {
+        // the queue of bounce b is paths[b & 1]: bounce 1 (every path length above 1) in paths[1],
+        // bounce 2 in paths[0], bounce 3 in paths[1] again
+        const size_t paths = MB > 1 ? (size_t)M * N : 1;
+        c->lp.paths[1] = dalloc<float4>(MB > 1 ? 4 * paths : 4);
+        c->lp.paths[0] = dalloc<float4>(MB > 2 ? 4 * paths : 4);
+        c->lp.pcount = dalloc<int>(MB + 1);
+        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train ||
+            !c->lp.paths[0] || !c->lp.paths[1] || !c->lp.pcount) {
             free_lp(c);
             c->err = "out of device memory (learned-target buffers)";
             return VR_ERR_OOM;
         }
         cudaMemset(c->lp.T, 0, slots * sizeof(float));
         cudaMemset(c->lp.qcount, 0, sizeof(int));
+        cudaMemset(c->lp.pcount, 0, (MB + 1) * sizeof(int));
         c->lp.qcapacity = (int)slots;
+        c->lp.pcapacity = (int)paths;
         c->lp.numSlots = M * MB;
         c->lp.trainCount = S;
         c->lpSlots = slots; c->lpM = M; c->lpMB = MB;
@@ -1590,6 +1601,13 @@ static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, 
 }
 
 template <int MB>
+static void launch_lp_bounce(const vrd::FrameParams& P, const vrd::LpBuffers& L, int bounce, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_lp_bounce_1(P, L, bounce, grid, st);
+    else if (MB == 2) vrk::launch_lp_bounce_2(P, L, bounce, grid, st);
+    else if (MB == 3) vrk::launch_lp_bounce_3(P, L, bounce, grid, st);
+    else vrk::launch_lp_bounce_4(P, L, bounce, grid, st);
+}
+template <int MB>
 static void launch_lp_generate(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
     if (MB == 1) vrk::launch_lp_generate_1(P, B, L, g, b, st);
     else if (MB == 2) vrk::launch_lp_generate_2(P, B, L, g, b, st);
@@ -1660,8 +1678,11 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     const bool lpOn = lp_active(c);
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+        cudaMemsetAsync(c->lp.pcount, 0, (MB + 1) * sizeof(int), st);
         VR_RANGE("vr.generate");
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
+        for (int b = 1; b < MB; ++b) launch_lp_bounce<MB>(P, c->lp, b, c->numSMs * VR_KINIT_MIN_BLOCKS, st);
+        c->launches += MB - 1;
         VR_RANGE_END();
         rec();
         VR_RANGE("vr.infer");
@@ -1939,7 +1960,8 @@ void noalloc_error(vr_context* c, const char* msg) { c->err = msg; }
 namespace vrk {
 #define VR_BDECL(MB)                                                                      \
     void launch_batch_pass_##MB(const vrd::BatchLaunch&, int, int, cudaStream_t);       \
-    void launch_batch_train_gen_##MB(const vrd::BatchLaunch&, int, cudaStream_t);
+    void launch_batch_train_gen_##MB(const vrd::BatchLaunch&, int, cudaStream_t);        \
+    void launch_batch_lp_bounce_##MB(const vrd::BatchLaunch&, int, int, int, cudaStream_t);
 VR_BDECL(1) VR_BDECL(2) VR_BDECL(3) VR_BDECL(4)
 #undef VR_BDECL
 }  // namespace vrk
@@ -1986,6 +2008,13 @@ static void batch_pass(const vrd::BatchLaunch& BL, int pass, int grid, cudaStrea
     else if (MB == 2) vrk::launch_batch_pass_2(BL, pass, grid, st);
     else if (MB == 3) vrk::launch_batch_pass_3(BL, pass, grid, st);
     else vrk::launch_batch_pass_4(BL, pass, grid, st);
+}
+template <int MB>
+static void batch_lp_bounce(const vrd::BatchLaunch& BL, int inst, int bounce, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_lp_bounce_1(BL, inst, bounce, grid, st);
+    else if (MB == 2) vrk::launch_batch_lp_bounce_2(BL, inst, bounce, grid, st);
+    else if (MB == 3) vrk::launch_batch_lp_bounce_3(BL, inst, bounce, grid, st);
+    else vrk::launch_batch_lp_bounce_4(BL, inst, bounce, grid, st);
 }
 template <int MB>
 static void batch_train_gen(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
@@ -2124,9 +2153,18 @@ static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
     if (anyPlain) { batch_pass<MB>(BL, 0, grid, st); launches++; }
     if (anyLearned) {
         for (vr_context* c : b->ctx)
-            if (lp_active(c)) cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+            if (lp_active(c)) {
+                cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
+                cudaMemsetAsync(c->lp.pcount, 0, (MB + 1) * sizeof(int), st);
+            }
         batch_pass<MB>(BL, 1, grid, st);
         launches++;
+        for (int i = 0; i < n; ++i)
+            if (lp_active(b->ctx[i]))
+                for (int bn = 1; bn < MB; ++bn) {
+                    batch_lp_bounce<MB>(BL, i, bn, grid, st);
+                    launches++;
+                }
         for (vr_context* c : b->ctx)
             if (lp_active(c)) {
                 vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);

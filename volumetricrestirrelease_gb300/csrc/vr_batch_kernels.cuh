@@ -66,6 +66,21 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_pixels(const Batc
     }
 }
 
+// the bounce pass b of learned instance `inst` (its queue of continuing candidate paths)
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_lp_bounce(const BatchLaunch BL, int inst, int b) {
+    __shared__ FrameParams sP;
+    __shared__ LpBuffers sL;
+    const BatchInstance& I = BL.inst[inst];
+    blockCopy(&c_scene, I.scene);
+    blockCopy(&sP, &I.P);
+    blockCopy(&sL, &I.L);
+    __syncthreads();
+    const int n = min(sL.pcount[b], sL.pcapacity);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x)
+        lpBouncePath<MB>(sP, sL, b, i);
+}
+
 // training samples of every learned instance, in chunks of 128 that never straddle instances
 template <int MB>
 __global__ void __launch_bounds__(128) kb_train_gen(const BatchLaunch BL) {

@@ -3,10 +3,12 @@
 //
 // With the learned target the initial pass runs in three steps so that the network is
 // evaluated on the tensor cores in batches:
-//   generate : every candidate path is sampled exactly as in the plain pass, except that the
-//              light visibility of each next-event estimate is not marched; the vertex's
-//              reservoir fields, its resampling uniform and (where the target needs it) a
-//              transmittance query (x, w, tmax, slot) are written out;
+//   generate : every candidate path is sampled as in the plain pass, except that the light
+//              visibility of each next-event estimate is not marched; the vertex's reservoir
+//              fields, its resampling uniform and (where the target needs it) a transmittance
+//              query (x, w, tmax, slot) are written out.  The first vertices come from one
+//              per-pixel kernel, the indirect vertices from one pass per bounce over a queue of
+//              the paths that go on (each candidate's indirect vertices use its own stream);
 //   infer    : the network predicts T for the compacted list of query slots;
 //   select   : the recorded candidates are resampled with p_hat = p_hat_unoccluded * T, then the
 //              pass continues as the plain one (p_hat of the winner, temporal reuse).
@@ -42,6 +44,9 @@ struct LpBuffers {
     int* qcount;
     int qcapacity;
     uint4* rng;        // [N]: the pixel's random state after generation
+    float4* paths[2];  // queues of continuing candidate paths, 4 float4 each (the bounce b queue is paths[b & 1])
+    int* pcount;       // [MB]: queue lengths by bounce
+    int pcapacity;     // entries of each queue (M * N)
     float4* train;     // [S][2]: (x, y, z, wx), (wy, wz, tmax or -1 when invalid, target)
     int trainCount;
     int numSlots;      // M * MB

@@ -43,145 +43,177 @@ __device__ __forceinline__ void lpAppendQuery(const LpBuffers& L, f3 x, f3 w, fl
     }
 }
 
-// one candidate path; writes the vertex records of candidate c of pixel pid and returns the
-// primary scattering depth
-template <int MB>
-static __device__ __noinline__ float initialSampleLP(const FrameParams& P, Ray ray, float preHit, float prePdf, float preTr, vr::Rng& sg,
-                                                      const LpBuffers& L, int c, int pid) {
-    const SamplingOptions& o = P.initial;
-    const int N = P.N;
-    float pathPdf = 1.f, pathPHat = 1.f;
-    float primaryDepth = 0;
-    const f3 sigma_s = c_scene.sigma_s, sigma_a = c_scene.sigma_a;
-    const float sigma_t = c_scene.sigma_t;
-    int bounce = 0;
-    for (; bounce < MB; bounce++) {
-        Reservoir out = newReservoir();
-        out.M = 1;
-        float hitD, pdfDist = 0, Tr;
-        MediumInteraction mi;
-        if (bounce >= 1) {
-            int curMip = o.visibilityMipLevel;
-            if (P.useCoarser) curMip = min((o.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + c_scene.numMips - 1, curMip + 1);
-            float hd[4], pd[4], trs[4];
-            sampleDistances(ray, sg, o.visibilityUseLinearSampler != 0, curMip, 1, hd, pd, trs);
-            hitD = hd[0]; pdfDist = pd[0]; Tr = trs[0];
-        } else {
-            hitD = preHit; pdfDist = prePdf; Tr = preTr;
-        }
-        mi.p = at(ray, hitD); mi.wo = -ray.d; mi.g = c_scene.g; mi.valid = hitD != kRayTMax;
-        pathPdf *= pdfDist;
-        bool hitEmpty = false;
-        float density = 0.f;
-        if (bounce == 0) {
-            if (MB > 1) out.sampledPixel = encodeBounces(out.sampledPixel, 0);
-            out.depth = mi.valid ? hitD : kRayTMax;
-            primaryDepth = out.depth;
-        } else {
-            if (MB > 1) {
-                out.sampledPixel = encodeBounces(out.sampledPixel, bounce);
-                f3 w = mk3(ray.d.x, ray.d.y, !mi.valid ? kRayTMax : hitD);
-                if (ray.d.z < 0) w.z = -w.z;
-                L.ex[(size_t)(c * (MB - 1) + bounce - 1) * N + pid] = make_float4(w.x, w.y, w.z, 0.f);
-            }
-        }
-        out.p_y = pathPdf;
-        if (mi.valid) density = densityWorld(mi.p, 0);
-        if ((!mi.valid && bounce > 0) || (mi.valid && density == 0)) {
-            out.p_y = 0.f; out.runningSum = 0.f; hitEmpty = true;
-        }
-        int flags = kLpValid;
-        float pdfDir = 1.f;
-        if (!hitEmpty) {
-            if (mi.valid) {
-                f3 albedo = sigma_s / sigma_t;
-                out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
-                float lightPdf = 0.f;
-                const bool emitting = c_scene.hasEmission && density > 0.f;
-                f3 Le = mk3(0.f);
-                if (emitting) Le = emissionWorld(mi.p);
-                f3 oma = mk3(1.f) - albedo;
-                LightSample ls;
-                const bool lv = sampleLights(mi.p, o.useEnvironmentLights != 0, o.useAnalyticLights != 0, sg, ls, out.lightID, out.uv0, out.uv1);
-                f3 Ld = mk3(0.f);
-                if (lv) {
-                    lightPdf = ls.pdfArea;
-                    float ph = phaseF(mi, mi.wo, ls.dir);
-                    Ld = mk3(0.f) + ph * ls.Li / 1.f;
-                }
-                f3 wo = -ray.d, wi = mk3(0.f);
-                if (MB > 1) {
-                    float u0 = vr::next1D(sg), u1 = vr::next1D(sg);
-                    pdfDir = samplePhase(mi, wo, wi, u0, u1);
-                }
-                float p_src = out.p_y;
-                {
-                    float er = 0.f;      // 0 without emission (see initialSample)
-                    if (emitting) {
-                        er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
-                        if (vr::isnan_(er)) er = 0.f;
-                    }
-                    if (vr::next1D(sg) < er) { p_src *= er; out.lightID = kSelfEmissionLightID; }
-                    else p_src *= lightPdf * (1 - er);
-                }
-                out.runningSum = p_src == 0.f ? 0.f : 1.f;
-                out.p_y = p_src;
-                {
-                    float p_y;
-                    pathPHat *= Tr;
-                    pathPHat *= density;
-                    const bool emis = out.lightID == kSelfEmissionLightID;
-                    if (emis) p_y = pathPHat * vr::luminance(sigma_a * Le);
-                    else p_y = pathPHat * vr::luminance(sigma_s * Ld * lightPdf);
-                    pathPHat *= vr::luminance(sigma_s) * pdfDir;
-                    if (out.runningSum > 0.f) {
-                        if (!emis && lv && o.lightSamples != 0 && p_y != 0.f) {
-                            // runningSum keeps p_src and p_y the unoccluded target until T is known
-                            flags |= kLpNeedsT;
-                            out.runningSum = out.p_y;
-                            out.p_y = p_y;
-                            lpAppendQuery(L, mi.p, ls.dir, ls.distance, (c * MB + bounce) * N + pid);
-                        } else {
-                            out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
-                            if (emis && bounce > 0) {
-                                out.lightID = vr::asint(mi.p.z); out.uv0 = mi.p.x; out.uv1 = mi.p.y;
-                                p_y /= (hitD * hitD);
-                                out.sampledPixel = encodeTag(out.sampledPixel, 1);
-                            }
-                            out.p_y = p_y;
-                        }
-                    }
-                }
-                pathPdf *= pdfDir;
-                if (MB > 1) {
-                    if (bounce < MB - 1) {
-                        ray = Ray{mi.p, wi, 0, kRayTMax};
-                        if (P.useRR && bounce >= 2) {
-                            if (vr::next1D(sg) < albedo.x) pathPdf *= albedo.x;
-                            else hitEmpty = true;
-                        }
-                    }
-                }
-            } else {
-                f3 Le = envEval(ray.d);
-                pathPHat *= Tr;
-                float p_y = pathPHat * vr::luminance(Le);
-                out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
-                out.p_y = p_y;
-                hitEmpty = true;
-            }
-        }
-        const float ub = MB > 1 ? vr::next1D(sg) : 0.f;
-        const size_t slot = (size_t)(c * MB + bounce) * N + pid;
-        L.vrecA[slot] = make_float4(out.runningSum, out.p_y, out.uv0, out.uv1);
-        L.vrecB[slot] = make_int4(out.lightID, out.sampledPixel, flags, __float_as_int(ub));
-        if (hitEmpty) { bounce++; break; }
-    }
-    if (bounce < MB) L.vrecB[(size_t)(c * MB + bounce) * N + pid].z = 0;
-    return primaryDepth;
+// state of one candidate path between its vertices
+struct LpPath {
+    Ray ray;
+    float pathPdf, pathPHat, primaryDepth;
+    int bounce;
+};
+
+// random stream of candidate c's indirect vertices (bounces >= 1); the pixel's own stream covers
+// the primary distance samples, the first vertex of every candidate and the candidate uniforms
+__device__ __forceinline__ vr::Rng lpCandidateStream(int px, int py, int frameCount, int c) {
+    return vr::rng_create((uint32_t)px, (uint32_t)py, 0x40000000u | (((uint32_t)frameCount * 4096u + (uint32_t)c) & 0x3FFFFFFFu));
 }
 
-// generate: GenerateFeatures + the candidates of TraceRays, recorded
+// a continuing path in the queue of its next bounce: (o, pathPdf), (d, pathPHat), (pixel,
+// candidate, -, -), the candidate stream
+__device__ __forceinline__ void lpEnqueue(const LpBuffers& L, int level, const LpPath& cs, int pid, int c, const vr::Rng& g) {
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    const int rank = __popc(m & ((1u << lane) - 1u));
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&L.pcount[level], __popc(m));
+    base = __shfl_sync(m, base, leader);
+    const size_t i = (size_t)(base + rank);
+    if (i >= (size_t)L.pcapacity) {                 // cannot happen: a candidate enters each queue once
+        if (c_scene.status) atomicOr(c_scene.status, 2);
+        return;
+    }
+    float4* q = L.paths[level & 1] + 4 * i;
+    q[0] = make_float4(cs.ray.o.x, cs.ray.o.y, cs.ray.o.z, cs.pathPdf);
+    q[1] = make_float4(cs.ray.d.x, cs.ray.d.y, cs.ray.d.z, cs.pathPHat);
+    q[2] = make_float4(__int_as_float(pid), __int_as_float(c), 0.f, 0.f);
+    q[3] = make_float4(__uint_as_float(g.s[0]), __uint_as_float(g.s[1]), __uint_as_float(g.s[2]), __uint_as_float(g.s[3]));
+}
+
+
+// one vertex (bounce cs.bounce) of candidate c: writes its record and returns true when the
+// path continues, i.e. when the next vertex needs a distance sample along cs.ray
+template <int MB>
+__device__ __forceinline__ bool lpVertex(const FrameParams& P, LpPath& cs, float hitD, float pdfDist, float Tr, vr::Rng& sg,
+                                         const LpBuffers& L, int c, int pid) {
+    const SamplingOptions& o = P.initial;
+    const int N = P.N;
+    const f3 sigma_s = c_scene.sigma_s, sigma_a = c_scene.sigma_a;
+    const float sigma_t = c_scene.sigma_t;
+    const int bounce = cs.bounce;
+    const Ray ray = cs.ray;
+    Reservoir out = newReservoir();
+    out.M = 1;
+    MediumInteraction mi;
+    mi.p = at(ray, hitD); mi.wo = -ray.d; mi.g = c_scene.g; mi.valid = hitD != kRayTMax;
+    cs.pathPdf *= pdfDist;
+    bool hitEmpty = false;
+    float density = 0.f;
+    if (bounce == 0) {
+        if (MB > 1) out.sampledPixel = encodeBounces(out.sampledPixel, 0);
+        out.depth = mi.valid ? hitD : kRayTMax;
+        cs.primaryDepth = out.depth;
+    } else {
+        if (MB > 1) {
+            out.sampledPixel = encodeBounces(out.sampledPixel, bounce);
+            f3 w = mk3(ray.d.x, ray.d.y, !mi.valid ? kRayTMax : hitD);
+            if (ray.d.z < 0) w.z = -w.z;
+            L.ex[(size_t)(c * (MB - 1) + bounce - 1) * N + pid] = make_float4(w.x, w.y, w.z, 0.f);
+        }
+    }
+    out.p_y = cs.pathPdf;
+    if (mi.valid) density = densityWorld(mi.p, 0);
+    if ((!mi.valid && bounce > 0) || (mi.valid && density == 0)) {
+        out.p_y = 0.f; out.runningSum = 0.f; hitEmpty = true;
+    }
+    int flags = kLpValid;
+    float pdfDir = 1.f;
+    if (!hitEmpty) {
+        if (mi.valid) {
+            f3 albedo = sigma_s / sigma_t;
+            out.lightID = -1; out.uv0 = 0; out.uv1 = 0;
+            float lightPdf = 0.f;
+            const bool emitting = c_scene.hasEmission && density > 0.f;
+            f3 Le = mk3(0.f);
+            if (emitting) Le = emissionWorld(mi.p);
+            f3 oma = mk3(1.f) - albedo;
+            LightSample ls;
+            const bool lv = sampleLights(mi.p, o.useEnvironmentLights != 0, o.useAnalyticLights != 0, sg, ls, out.lightID, out.uv0, out.uv1);
+            f3 Ld = mk3(0.f);
+            if (lv) {
+                lightPdf = ls.pdfArea;
+                float ph = phaseF(mi, mi.wo, ls.dir);
+                Ld = mk3(0.f) + ph * ls.Li / 1.f;
+            }
+            f3 wo = -ray.d, wi = mk3(0.f);
+            if (MB > 1) {
+                float u0 = vr::next1D(sg), u1 = vr::next1D(sg);
+                pdfDir = samplePhase(mi, wo, wi, u0, u1);
+            }
+            float p_src = out.p_y;
+            {
+                float er = 0.f;      // 0 without emission (see initialSample)
+                if (emitting) {
+                    er = vr::luminance(oma * Le) / (vr::luminance(oma * Le) + vr::luminance(albedo * Ld));
+                    if (vr::isnan_(er)) er = 0.f;
+                }
+                if (vr::next1D(sg) < er) { p_src *= er; out.lightID = kSelfEmissionLightID; }
+                else p_src *= lightPdf * (1 - er);
+            }
+            out.runningSum = p_src == 0.f ? 0.f : 1.f;
+            out.p_y = p_src;
+            {
+                float p_y;
+                cs.pathPHat *= Tr;
+                cs.pathPHat *= density;
+                const bool emis = out.lightID == kSelfEmissionLightID;
+                if (emis) p_y = cs.pathPHat * vr::luminance(sigma_a * Le);
+                else p_y = cs.pathPHat * vr::luminance(sigma_s * Ld * lightPdf);
+                cs.pathPHat *= vr::luminance(sigma_s) * pdfDir;
+                if (out.runningSum > 0.f) {
+                    if (!emis && lv && o.lightSamples != 0 && p_y != 0.f) {
+                        // runningSum keeps p_src and p_y the unoccluded target until T is known
+                        flags |= kLpNeedsT;
+                        out.runningSum = out.p_y;
+                        out.p_y = p_y;
+                        lpAppendQuery(L, mi.p, ls.dir, ls.distance, (c * MB + bounce) * N + pid);
+                    } else {
+                        out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+                        if (emis && bounce > 0) {
+                            out.lightID = vr::asint(mi.p.z); out.uv0 = mi.p.x; out.uv1 = mi.p.y;
+                            p_y /= (hitD * hitD);
+                            out.sampledPixel = encodeTag(out.sampledPixel, 1);
+                        }
+                        out.p_y = p_y;
+                    }
+                }
+            }
+            cs.pathPdf *= pdfDir;
+            if (MB > 1) {
+                if (bounce < MB - 1) {
+                    cs.ray = Ray{mi.p, wi, 0, kRayTMax};
+                    if (P.useRR && bounce >= 2) {
+                        if (vr::next1D(sg) < albedo.x) cs.pathPdf *= albedo.x;
+                        else hitEmpty = true;
+                    }
+                }
+            }
+        } else {
+            f3 Le = envEval(ray.d);
+            cs.pathPHat *= Tr;
+            float p_y = cs.pathPHat * vr::luminance(Le);
+            out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
+            out.p_y = p_y;
+            hitEmpty = true;
+        }
+    }
+    const float ub = MB > 1 ? vr::next1D(sg) : 0.f;
+    const size_t slot = (size_t)(c * MB + bounce) * N + pid;
+    L.vrecA[slot] = make_float4(out.runningSum, out.p_y, out.uv0, out.uv1);
+    L.vrecB[slot] = make_int4(out.lightID, out.sampledPixel, flags, __float_as_int(ub));
+    // the record after the last vertex of a path that ended early is marked invalid
+    if (hitEmpty) {
+        if (bounce + 1 < MB) L.vrecB[(size_t)(c * MB + bounce + 1) * N + pid].z = 0;
+        return false;
+    }
+    cs.bounce = bounce + 1;
+    return cs.bounce < MB;
+}
+
+// generate, in the wavefront order of the learned target: GenerateFeatures, then per pixel the
+// rounds of TraceRays (up to 4 primary distance samples in one traversal) and the first vertex
+// of every candidate, all from the pixel's stream (neighbouring camera rays walk the same bricks
+// together); a candidate whose path continues is queued for the bounce passes, which draw from
+// the candidate's own stream.  Queuing the indirect vertices keeps every lane of a bounce pass
+// on a live path, where the per-pixel loop left most lanes waiting on the few paths that go on.
 template <int MB>
 __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
     const int W = P.W, H = P.H, N = P.N;
@@ -198,13 +230,46 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
         int rs = rd == rounds - 1 ? (M - 4 * (rounds - 1)) : 4;
         sampleDistances(ray, sg, P.initial.visibilityUseLinearSampler != 0, P.initial.visibilityMipLevel, rs, hd, pd, trs);
         for (int s = 0; s < rs; s++, c++) {
-            float depth = initialSampleLP<MB>(P, ray, hd[s], pd[s], trs[s], sg, L, c, pid);
-            float uc = vr::next1D(sg);
-            L.crec[(size_t)c * N + pid] = make_float2(depth, uc);
+            LpPath cs;
+            cs.ray = ray; cs.pathPdf = 1.f; cs.pathPHat = 1.f; cs.primaryDepth = 0.f; cs.bounce = 0;
+            const bool more = lpVertex<MB>(P, cs, hd[s], pd[s], trs[s], sg, L, c, pid);
+            const float uc = vr::next1D(sg);
+            L.crec[(size_t)c * N + pid] = make_float2(cs.primaryDepth, uc);
+            if (more) lpEnqueue(L, 1, cs, pid, c, lpCandidateStream(px, py, P.frameCount, c));
         }
     }
     L.rng[pid] = make_uint4(sg.s[0], sg.s[1], sg.s[2], sg.s[3]);
     (void)H;
+}
+
+// one indirect vertex (bounce b >= 1) of a queued path: its distance sample, then the vertex;
+// a path that goes on is queued for bounce b + 1
+template <int MB>
+__device__ __forceinline__ void lpBouncePath(const FrameParams& P, const LpBuffers& L, int b, size_t i) {
+    const float4* q = L.paths[b & 1] + 4 * i;
+    const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+    LpPath cs;
+    cs.ray = Ray{mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), 0.f, kRayTMax};
+    cs.pathPdf = q0.w; cs.pathPHat = q1.w; cs.primaryDepth = 0.f; cs.bounce = b;
+    const int pid = __float_as_int(q2.x), c = __float_as_int(q2.y);
+    vr::Rng g;
+    g.s[0] = __float_as_uint(q3.x); g.s[1] = __float_as_uint(q3.y); g.s[2] = __float_as_uint(q3.z); g.s[3] = __float_as_uint(q3.w);
+    const SamplingOptions& o = P.initial;
+    int curMip = o.visibilityMipLevel;
+    if (P.useCoarser) curMip = min((o.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + c_scene.numMips - 1, curMip + 1);
+    float hd[4], pd[4], trs[4];
+    sampleDistances(cs.ray, g, o.visibilityUseLinearSampler != 0, curMip, 1, hd, pd, trs);
+    if (lpVertex<MB>(P, cs, hd[0], pd[0], trs[0], g, L, c, pid)) lpEnqueue(L, b + 1, cs, pid, c, g);
+}
+
+// the bounce pass b: a persistent grid over the queue of bounce b, whose length the previous pass
+// left on the device
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_bounce(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L,
+                                                                        int b) {
+    const int n = min(L.pcount[b], L.pcapacity);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x)
+        lpBouncePath<MB>(P, L, b, i);
 }
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
