@@ -657,7 +657,9 @@ def run_gpu(args):
         alg = per_px * W * H
         achieved = alg / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": _traffic_from_profile("k_lp_generate"), "kernel": "k_lp_generate", "peak_source": peak_kind,
+                "traffic": _traffic_from_profile("k_lp_generate"),
+                "kernel": "k_lp_generate + k_lp_bounce (the generate stage: one per-pixel launch, then one launch per bounce)",
+                "peak_source": peak_kind,
                 "dominant_by_time": dom, "algorithmic_bytes_per_launch": alg, "algorithmic_bytes_per_pixel": per_px,
                 "voxel_reads_per_pixel": lpc["generate_voxel_reads_px"], "vertex_records_per_pixel": lpc["vertices_px"],
                 "queries_per_pixel": lpc["queries_px"], "kernel_ms": kernel_ms["k_lp_generate"],
