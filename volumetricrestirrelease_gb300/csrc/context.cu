@@ -43,7 +43,8 @@ namespace vrk {
     void launch_lp_generate_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
     void launch_lp_select_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
     void launch_lp_train_gen_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, uint32_t, cudaStream_t);          \
-    void launch_lp_bounce_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, int, int, cudaStream_t);
+    void launch_lp_bounce_##MB(const vrd::FrameParams&, const vrd::LpBuffers&, int, int, int, cudaStream_t);      \
+    void launch_lp_sort_##MB(const vrd::LpBuffers&, int, int, cudaStream_t);
 VR_DECL(1) VR_DECL(2) VR_DECL(3) VR_DECL(4)
 #undef VR_DECL
 // the network kernels (lp.cu)
@@ -353,7 +354,7 @@ static int alloc_buffers(vr_context* c) {
 static void free_lp(vr_context* c) {
     cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.ex); cudaFree(c->lp.T);
     cudaFree(c->lp.query); cudaFree(c->lp.qlist); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
-    cudaFree(c->lp.paths[0]); cudaFree(c->lp.paths[1]); cudaFree(c->lp.pcount);
+    cudaFree(c->lp.paths[0]); cudaFree(c->lp.paths[1]); cudaFree(c->lp.pcount); cudaFree(c->lp.psort); cudaFree(c->lp.hist);
     c->lp = vrd::LpBuffers{};
     c->lpSlots = 0; c->lpM = 0; c->lpMB = 0;
 }
@@ -477,9 +478,11 @@ static int lp_alloc(vr_context* c) {
         const size_t paths = MB > 1 ? (size_t)M * N : 1;
         c->lp.paths[1] = dalloc<float4>(MB > 1 ? 4 * paths : 4);
         c->lp.paths[0] = dalloc<float4>(MB > 2 ? 4 * paths : 4);
+        c->lp.psort = dalloc<float4>(4 * paths);
+        c->lp.hist = dalloc<int>(2 * vrd::kPathKeys);
         c->lp.pcount = dalloc<int>(MB + 1);
         if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train ||
-            !c->lp.paths[0] || !c->lp.paths[1] || !c->lp.pcount) {
+            !c->lp.paths[0] || !c->lp.paths[1] || !c->lp.pcount || !c->lp.psort || !c->lp.hist) {
             free_lp(c);
             c->err = "out of device memory (learned-target buffers)";
             return VR_ERR_OOM;
@@ -1602,10 +1605,11 @@ static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, 
 
 template <int MB>
 static void launch_lp_bounce(const vrd::FrameParams& P, const vrd::LpBuffers& L, int bounce, int grid, cudaStream_t st) {
-    if (MB == 1) vrk::launch_lp_bounce_1(P, L, bounce, grid, st);
-    else if (MB == 2) vrk::launch_lp_bounce_2(P, L, bounce, grid, st);
-    else if (MB == 3) vrk::launch_lp_bounce_3(P, L, bounce, grid, st);
-    else vrk::launch_lp_bounce_4(P, L, bounce, grid, st);
+    // sort the queue by coherence key, then the bounce pass over the sorted copy
+    if (MB == 1) { vrk::launch_lp_sort_1(L, bounce, grid, st); vrk::launch_lp_bounce_1(P, L, bounce, grid, 1, st); }
+    else if (MB == 2) { vrk::launch_lp_sort_2(L, bounce, grid, st); vrk::launch_lp_bounce_2(P, L, bounce, grid, 1, st); }
+    else if (MB == 3) { vrk::launch_lp_sort_3(L, bounce, grid, st); vrk::launch_lp_bounce_3(P, L, bounce, grid, 1, st); }
+    else { vrk::launch_lp_sort_4(L, bounce, grid, st); vrk::launch_lp_bounce_4(P, L, bounce, grid, 1, st); }
 }
 template <int MB>
 static void launch_lp_generate(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b, cudaStream_t st) {
@@ -1679,10 +1683,11 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
         cudaMemsetAsync(c->lp.pcount, 0, (MB + 1) * sizeof(int), st);
+        for (int k = 0; k < 3; ++k) { c->lp.kmin[k] = c->netBmin[k]; c->lp.kinv[k] = c->netBinv[k]; }
         VR_RANGE("vr.generate");
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
         for (int b = 1; b < MB; ++b) launch_lp_bounce<MB>(P, c->lp, b, c->numSMs * VR_KINIT_MIN_BLOCKS, st);
-        c->launches += MB - 1;
+        c->launches += 4 * (MB - 1);
         VR_RANGE_END();
         rec();
         VR_RANGE("vr.infer");

@@ -38,8 +38,15 @@ void VR_CAT(launch_lp_select_, VR_MB)(const vrd::FrameParams& P, const vrd::Fram
                                       cudaStream_t st) {
     vrd::k_lp_select<VR_MB><<<g, b, 0, st>>>(P, B, L);
 }
-void VR_CAT(launch_lp_bounce_, VR_MB)(const vrd::FrameParams& P, const vrd::LpBuffers& L, int b, int grid, cudaStream_t st) {
-    vrd::k_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(P, L, b);
+void VR_CAT(launch_lp_bounce_, VR_MB)(const vrd::FrameParams& P, const vrd::LpBuffers& L, int b, int grid, int sorted, cudaStream_t st) {
+    vrd::k_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(P, L, b, sorted);
+}
+// counting sort of the queue of bounce b into L.psort
+void VR_CAT(launch_lp_sort_, VR_MB)(const vrd::LpBuffers& L, int b, int grid, cudaStream_t st) {
+    cudaMemsetAsync(L.hist, 0, vrd::kPathKeys * sizeof(int), st);
+    vrd::k_path_hist<<<grid, 256, 0, st>>>(L, b);
+    vrd::k_path_scan<<<1, 1024, 0, st>>>(L);
+    vrd::k_path_scatter<<<grid, 256, 0, st>>>(L, b);
 }
 void VR_CAT(launch_lp_train_gen_, VR_MB)(const vrd::FrameParams& P, const vrd::LpBuffers& L, uint32_t seed, cudaStream_t st) {
     vrd::k_lp_train_gen<VR_MB><<<(L.trainCount + 127) / 128, 128, 0, st>>>(P, L, seed);

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_lp_bounce(const B
     __syncthreads();
     const int n = min(sL.pcount[b], sL.pcapacity);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x)
-        lpBouncePath<MB>(sP, sL, b, i);
+        lpBouncePath<MB>(sP, sL, b, sL.paths[b & 1], i);
 }
 
 // training samples of every learned instance, in chunks of 128 that never straddle instances

@@ -20,6 +20,9 @@
 
 namespace vrd {
 
+// coherence keys of the path-queue sort: ray octant x 8^3 origin cell
+constexpr int kPathKeys = 4096;
+
 struct NetView {
     const uint16_t* wbf;   // BF16 weights: 4 hidden matrices [64 out][64 in] then the 64 output weights
     const float* bias;     // FP32 biases: 4 x 64 hidden, then the output bias
@@ -47,6 +50,9 @@ struct LpBuffers {
     float4* paths[2];  // queues of continuing candidate paths, 4 float4 each (the bounce b queue is paths[b & 1])
     int* pcount;       // [MB]: queue lengths by bounce
     int pcapacity;     // entries of each queue (M * N)
+    float4* psort;     // a queue sorted by coherence key before its bounce pass (single-context frames)
+    int* hist;         // [2][kPathKeys]: key counts, then scatter cursors
+    float kmin[3], kinv[3];   // the volume's world box: key cell = floor(8 * (x - kmin) * kinv)
     float4* train;     // [S][2]: (x, y, z, wx), (wy, wz, tmax or -1 when invalid, target)
     int trainCount;
     int numSlots;      // M * MB

@@ -242,11 +242,11 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
     (void)H;
 }
 
-// one indirect vertex (bounce b >= 1) of a queued path: its distance sample, then the vertex;
-// a path that goes on is queued for bounce b + 1
+// one indirect vertex (bounce b >= 1) of a queued path (entry i of `src`): its distance sample,
+// then the vertex; a path that goes on is queued for bounce b + 1
 template <int MB>
-__device__ __forceinline__ void lpBouncePath(const FrameParams& P, const LpBuffers& L, int b, size_t i) {
-    const float4* q = L.paths[b & 1] + 4 * i;
+__device__ __forceinline__ void lpBouncePath(const FrameParams& P, const LpBuffers& L, int b, const float4* src, size_t i) {
+    const float4* q = src + 4 * i;
     const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
     LpPath cs;
     cs.ray = Ray{mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), 0.f, kRayTMax};
@@ -262,14 +262,74 @@ __device__ __forceinline__ void lpBouncePath(const FrameParams& P, const LpBuffe
     if (lpVertex<MB>(P, cs, hd[0], pd[0], trs[0], g, L, c, pid)) lpEnqueue(L, b + 1, cs, pid, c, g);
 }
 
-// the bounce pass b: a persistent grid over the queue of bounce b, whose length the previous pass
-// left on the device
+// the bounce pass b: a persistent grid over the queue of bounce b (or its sorted copy), whose
+// length the previous pass left on the device
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_bounce(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L,
-                                                                        int b) {
+                                                                        int b, int sorted) {
     const int n = min(L.pcount[b], L.pcapacity);
+    const float4* src = sorted ? L.psort : L.paths[b & 1];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x)
-        lpBouncePath<MB>(P, L, b, i);
+        lpBouncePath<MB>(P, L, b, src, i);
+}
+
+// Counting sort of a queue by coherence key before its bounce pass: the octant of the direction
+// and the 8^3 cell of the volume box holding the origin, so that a warp takes paths that cross
+// the same region in the same direction.  The order of a queue changes no result (every path
+// writes its own slots), only the divergence of the traversals in a warp.
+__device__ __forceinline__ int lpPathKey(const LpBuffers& L, float4 q0, float4 q1) {
+    int cell[3];
+    const float o[3] = {q0.x, q0.y, q0.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float u = (o[k] - L.kmin[k]) * L.kinv[k] * 8.f;
+        cell[k] = u >= 0.f ? (u < 8.f ? (int)u : 7) : 0;       // NaN lands in cell 0
+    }
+    const int oct = (q1.x < 0.f ? 1 : 0) | (q1.y < 0.f ? 2 : 0) | (q1.z < 0.f ? 4 : 0);
+    return (oct << 9) | (cell[2] << 6) | (cell[1] << 3) | cell[0];
+}
+static __global__ void __launch_bounds__(256) k_path_hist(const __grid_constant__ LpBuffers L, int b) {
+    __shared__ int h[kPathKeys];
+    for (int i = threadIdx.x; i < kPathKeys; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const int n = min(L.pcount[b], L.pcapacity);
+    const float4* q = L.paths[b & 1];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[lpPathKey(L, q[4 * i], q[4 * i + 1])], 1);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kPathKeys; i += blockDim.x)
+        if (h[i]) atomicAdd(&L.hist[i], h[i]);
+}
+// exclusive prefix sums of the key counts into the scatter cursors: one block of 1024 threads,
+// 4 keys each
+static __global__ void __launch_bounds__(1024) k_path_scan(const __grid_constant__ LpBuffers L) {
+    __shared__ int s[1024];
+    const int t = threadIdx.x;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { v[k] = L.hist[4 * t + k]; sum += v[k]; }
+    s[t] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        const int add = t >= off ? s[t - off] : 0;
+        __syncthreads();
+        s[t] += add;
+        __syncthreads();
+    }
+    int base = s[t] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { L.hist[kPathKeys + 4 * t + k] = base; base += v[k]; }
+}
+static __global__ void __launch_bounds__(256) k_path_scatter(const __grid_constant__ LpBuffers L, int b) {
+    const int n = min(L.pcount[b], L.pcapacity);
+    const float4* q = L.paths[b & 1];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 a = q[4 * i], c = q[4 * i + 1], d = q[4 * i + 2], e = q[4 * i + 3];
+        const int pos = atomicAdd(&L.hist[kPathKeys + lpPathKey(L, a, c)], 1);
+        if (pos < 0 || pos >= n) continue;                    // cannot happen: the cursors cover [0, n)
+        float4* o = L.psort + 4 * (size_t)pos;
+        o[0] = a; o[1] = c; o[2] = d; o[3] = e;
+    }
 }
 template <int MB>
 __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
