@@ -848,8 +848,14 @@ static __device__ __forceinline__ float computeVisibility(const Ray& ray, vr::Rn
     vis /= samples;
     return vis;
 }
+// The learned form's generate and bounce kernels track with their own adapter type, so that
+// they call their own instance of the (noinline) traversal rather than the one the other
+// kernels of the unit share: measured 3 ms faster per 1080p learned frame (136.9-137.2 ->
+// 133.7-133.8 ms), with bit-identical images.
+struct SampleDistLp : SampleDist {};
+template <class SD = SampleDist>
 __device__ inline void sampleDistances(const Ray& r, vr::Rng& sg, bool lin, int mip, int n, float hit[4], float pdf[4], float tr[4]) {
-    SampleDist a; a.n = n; a.lin = lin;
+    SD a; a.n = n; a.lin = lin;
     if (lin) for (int i = 0; i < n; i++) a.tr[i] = -vr::log_(1 - vr::next1D(sg));
     trackVolume(r, mip, sg, a, lin);
     for (int i = 0; i < 4; ++i) { hit[i] = a.hit[i]; pdf[i] = a.pdf[i]; tr[i] = a.tr[i]; }

@@ -228,7 +228,7 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
     for (int rd = 0; rd < rounds; rd++) {
         float hd[4] = {0, 0, 0, 0}, pd[4] = {0, 0, 0, 0}, trs[4] = {0, 0, 0, 0};
         int rs = rd == rounds - 1 ? (M - 4 * (rounds - 1)) : 4;
-        sampleDistances(ray, sg, P.initial.visibilityUseLinearSampler != 0, P.initial.visibilityMipLevel, rs, hd, pd, trs);
+        sampleDistances<SampleDistLp>(ray, sg, P.initial.visibilityUseLinearSampler != 0, P.initial.visibilityMipLevel, rs, hd, pd, trs);
         for (int s = 0; s < rs; s++, c++) {
             LpPath cs;
             cs.ray = ray; cs.pathPdf = 1.f; cs.pathPHat = 1.f; cs.primaryDepth = 0.f; cs.bounce = 0;
@@ -258,7 +258,7 @@ __device__ __forceinline__ void lpBouncePath(const FrameParams& P, const LpBuffe
     int curMip = o.visibilityMipLevel;
     if (P.useCoarser) curMip = min((o.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + c_scene.numMips - 1, curMip + 1);
     float hd[4], pd[4], trs[4];
-    sampleDistances(cs.ray, g, o.visibilityUseLinearSampler != 0, curMip, 1, hd, pd, trs);
+    sampleDistances<SampleDistLp>(cs.ray, g, o.visibilityUseLinearSampler != 0, curMip, 1, hd, pd, trs);
     if (lpVertex<MB>(P, cs, hd[0], pd[0], trs[0], g, L, c, pid)) lpEnqueue(L, b + 1, cs, pid, c, g);
 }
 
