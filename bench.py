@@ -181,7 +181,7 @@ def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=10
     """relMSE of each form against an FP64 path-traced reference at QWxQH, static camera,
     averaged over frames first..frames-1, with the standard error of that mean from the means of
     blocks of `block` consecutive frames (consecutive frames are correlated through temporal
-    reuse).  forms: {name: (fp16, learned, M)} -> {name: (mean, standard error)}."""
+    reuse).  forms: {name: (fp16, learned, M[, volume key])} -> {name: (mean, standard error)}."""
     import torch
     from volumetricrestirrelease_gb300.restir import VolumetricReSTIR
     sc = _scene(args, static=True, width=QW, height=QH)
@@ -196,11 +196,13 @@ def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=10
     out = torch.empty((QH, QW, 4), device="cuda")
     res = {}
     plain_imgs = {}
-    vs_fp32 = None
-    for name, (fp16, learned, M) in forms.items():
+    vs_fp32 = {}
+    for name, form in forms.items():
+        fp16, learned, M = form[:3]
+        vkey = form[3] if len(form) > 3 else fp16
         scf = _scene(args, fp16=fp16, static=True, width=QW, height=QH)
         rd = VolumetricReSTIR(QW, QH, _options(lib, scf, learned, M).as_dict(), lib=lib)
-        rd.setScene(vols[fp16], scf.medium, scf.lights, scf.env_rgb, scf.env_scale)
+        rd.setScene(vols[vkey], scf.medium, scf.lights, scf.env_rgb, scf.env_scale)
         errs, cross = [], []
         for f in range(frames):
             rd.execute(scf.camera(f), out.data_ptr())
@@ -210,15 +212,15 @@ def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=10
                 errs.append(_relmse(img, ref))
                 if name == "plain":
                     plain_imgs[f] = img[..., :3].astype(np.float64)
-                elif name == "plain_fp16" and f in plain_imgs:
+                elif name in ("plain_fp16", "plain_bc4") and f in plain_imgs:
                     cross.append(_relmse(img, plain_imgs[f]))
         if cross:
-            vs_fp32 = float(np.mean(cross))
+            vs_fp32[name] = float(np.mean(cross))
         e = np.asarray(errs)
         bm = e[: len(e) // block * block].reshape(-1, block).mean(1)
         res[name] = (float(e.mean()), float(bm.std(ddof=1) / np.sqrt(len(bm))))
         del rd
-    return res, {"fp16_vs_fp32_relmse": vs_fp32, "resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
+    return res, {"fp16_vs_fp32_relmse": vs_fp32.get("plain_fp16"), "bc4_vs_fp32_relmse": vs_fp32.get("plain_bc4"), "resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
                  "reference": f"{spp} spp FP64 path tracer on the GPU", "relmse": "mean over pixels and RGB of (x-r)^2/(r^2+0.01)",
                  "standard_error": f"from the means of blocks of {block} frames"}
 
@@ -405,7 +407,8 @@ def run_batched(args, lib):
 
 
 def run_small_configs(args, lib):
-    """The 256^2 configurations: cfg1 (plain, FP32), cfg3 (FP16 bricks), cfg4 (learned target),
+    """The 256^2 configurations: cfg1 (plain, FP32), cfg3 (FP16 bricks, and BC4 coarse and
+    conservative mips), cfg4 (learned target),
     16 frames at the static camera of the small scene; relMSE of every frame against a 4096-spp
     FP64 reference, FP16 against FP32 frame by frame, frames/s, and the oracle on all host cores
     for cfg1."""
@@ -416,6 +419,7 @@ def run_small_configs(args, lib):
     W = H = 256
     sc32, sc16 = scenes.small(width=W, height=H), scenes.small(width=W, height=H, fp16=True)
     vol32, vol16 = Volume.procedural(sc32.volume, lib=lib), Volume.procedural(sc16.volume, lib=lib)
+    volbc4 = Volume.procedural(sc32.volume, lib=lib).compress_bc4()
 
     def ctx(sc, vol, learned=False):
         o = _options(lib, sc, learned)
@@ -432,7 +436,7 @@ def run_small_configs(args, lib):
     out = torch.empty((H, W, 4), device="cuda")
     res, imgs32 = {}, {}
     for name, sc, vol, learned in (("cfg1_plain_fp32", sc32, vol32, False), ("cfg3_plain_fp16", sc16, vol16, False),
-                                   ("cfg4_learned_fp32", sc32, vol32, True)):
+                                   ("cfg3_plain_bc4", sc32, volbc4, False), ("cfg4_learned_fp32", sc32, vol32, True)):
         r, o = ctx(sc, vol, learned)
         errs, cross = [], []
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -450,7 +454,7 @@ def run_small_configs(args, lib):
             errs.append(_relmse(img, ref))
             if name == "cfg1_plain_fp32":
                 imgs32[f] = img[..., :3].astype(np.float64)
-            elif name == "cfg3_plain_fp16":
+            elif name in ("cfg3_plain_fp16", "cfg3_plain_bc4"):
                 cross.append(_relmse(img, imgs32[f]))
         res[name] = {"frames_per_s": 1000.0 / ms, "relmse_per_frame": errs, "relmse_frames_8_15": float(np.mean(errs[8:]))}
         if cross:
@@ -553,6 +557,7 @@ def run_gpu(args):
     W, H = args.width, args.height
     t0 = time.time()
     vols = {False: Volume.procedural(_scene(args).volume, lib=lib), True: Volume.procedural(_scene(args, fp16=True).volume, lib=lib)}
+    vols["bc4"] = Volume.procedural(_scene(args).volume, lib=lib).compress_bc4()
     build_s = time.time() - t0
 
     def barrier():
@@ -560,7 +565,7 @@ def run_gpu(args):
             torch.distributed.barrier()
 
     # ---- relMSE matching (480x270, static camera, FP64 reference) ----
-    forms = {"plain": (False, False, 32), "plain_fp16": (True, False, 32)}
+    forms = {"plain": (False, False, 32), "plain_fp16": (True, False, 32), "plain_bc4": (False, False, 32, "bc4")}
     for M in LEARNED_M:
         forms[f"learned_M{M}"] = (True, True, M)
     rel, qinfo = quality(lib, vols, args, forms) if not args.no_quality else ({}, {})
@@ -628,6 +633,13 @@ def run_gpu(args):
     msp, kmsp, _, _ = _time_frames(rp, scp, out, sptr, args.warmup, args.steps, barrier=barrier)
     plain_fps = whole_job_rate(ws, args.steps, max_over_ranks(msp, ws))
     del rp
+    # ---- plain form on BC4 coarse and conservative mips (the reference's texture form) ----
+    rb = VolumetricReSTIR(W, H, optp.as_dict(), lib=lib)
+    rb.setScene(vols["bc4"], scp.medium, scp.lights, scp.env_rgb, scp.env_scale)
+    bc4_steps = min(args.steps, 8)
+    msb, kmsb, _, _ = _time_frames(rb, scp, out, sptr, args.warmup, bc4_steps, barrier=barrier)
+    bc4_fps = whole_job_rate(ws, bc4_steps, max_over_ranks(msb, ws))
+    del rb
 
     batched = None
     if not args.no_batched and rank == 0:
@@ -682,7 +694,9 @@ def run_gpu(args):
                        "training": {"samples_per_frame": opts.mLearnedTrainSamples, "batch": opts.mLearnedBatch,
                                     "lr": opts.mLearnedLearningRate}},
             "plain": {"value": plain_fps, "unit": "frames/s", "candidates": 32, "bricks": "fp32",
-                      "kernel_ms": {"k_initial": kmsp[0], "k_spatial": kmsp[1]}, "speedup_learned_vs_plain": value / plain_fps},
+                      "kernel_ms": {"k_initial": kmsp[0], "k_spatial": kmsp[1]}, "speedup_learned_vs_plain": value / plain_fps,
+                      "bc4": {"value": bc4_fps, "unit": "frames/s", "frames": bc4_steps, "kernel_ms": {"k_initial": kmsb[0], "k_spatial": kmsb[1]},
+                              "bricks": "mip 0 fp32; coarse and conservative mips BC4", "relmse": rel.get("plain_bc4")}},
             "relmse": {"matched": matched, "criterion": "learned - plain <= 2 standard errors of the difference",
                        "plain": rel.get("plain"), "learned": rel.get(f"learned_M{M_sel}"),
                        "all": {k: {"mean": v[0], "se": v[1]} for k, v in rel.items()}, **qinfo},

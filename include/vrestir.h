@@ -168,6 +168,8 @@ typedef struct vr_grid_view {
     const float* brick_bounds;    /* 4 floats per brick: min, max, avg(sum/512), 0 */
     const float* brick_f32;       /* 10^3 floats per brick (apron 1), or NULL */
     const uint16_t* brick_f16;    /* 10^3 halves per brick, or NULL */
+    const uint64_t* brick_bc4;    /* 90 BC4 blocks per brick, or NULL (vr_volume_compress_bc4) */
+    float bc4_scale;              /* density = decoded unorm value * bc4_scale */
 } vr_grid_view;
 
 typedef struct vr_volume_info {
@@ -179,6 +181,7 @@ typedef struct vr_volume_info {
     int64_t device_bytes;         /* bytes the grid occupies once bound to a context */
     int32_t fp16;
     float world_min[3];           /* world position of index-space corner (0, 0, 0) */
+    int32_t bc4;                  /* coarse and conservative mips stored as BC4 blocks */
 } vr_volume_info;
 
 typedef struct vr_point_light {   /* LightHelpers.slang:223-242 (point light, uniform emission) */
@@ -245,6 +248,13 @@ const char* vr_volume_vbx_error(void);
  * a voxel is nonzero, values stored as given.  values: res^3, x fastest. */
 int vr_volume_create_dense_signed(const float* values, int32_t res, const float world_min[3], float voxel_size,
                                   int32_t fp16, vr_volume** out);
+/* The reference's default texture form (Scene.cpp:3161-3181, ATLAS_COMPRESSION 2): normal mips
+ * 1.. and every conservative mip re-encoded as BC4 unorm blocks scaled by the slot's maximum
+ * (4x4 texels of each z-slice of a brick's 10^3 apron box, 90 blocks of 8 bytes per brick);
+ * normal mip 0 keeps its FP32 or FP16 storage.  Brick bounds are recomputed from the decoded
+ * values; on the conservative mips no nonzero voxel decodes to zero.  In place; a second call
+ * changes nothing. */
+int vr_volume_compress_bc4(vr_volume* v);
 void vr_volume_destroy(vr_volume* v);
 int vr_volume_get_info(const vr_volume* v, vr_volume_info* info);
 int vr_volume_get_slot(const vr_volume* v, int32_t slot, vr_grid_view* view);

@@ -19,6 +19,7 @@ def _load():
     sig = {
         "vro_create": (P, [P, C.c_int, C.c_int]),
         "vro_destroy": (None, [P]),
+        "vro_bc4_decode_block": (None, [C.c_uint64, P]),
         "vro_set_threads": (None, [P, C.c_int]),
         "vro_set_options": (None, [P, P]),
         "vro_set_volume": (C.c_int, [P, P, C.c_int, P, C.c_float, C.c_float, C.c_int]),

@@ -2489,6 +2489,32 @@ void vro_set_options(void* h, const vr_options* o) {
     p->optionsChanged = true;
 }
 
+// BC4 unorm block (the block layout of BCHelper.h:9-69, the format the reference's textures
+// use for the coarse and conservative mips, Scene.cpp:3161-3181): red_0 in bits 0-7, red_1 in
+// bits 8-15, texel t's 3-bit index at bit 16 + 3 t.  red_0 > red_1: entries red_0, red_1 and
+// (7 - k) red_0 + k red_1 over 7 for k = 1..6; otherwise red_0, red_1, (5 - k) red_0 + k red_1
+// over 5 for k = 1..4, then 0 and 1.  Each entry is its integer numerator (over 255 * 7 or
+// 255 * 5) times that denominator's reciprocal rounded to float.
+static float bc4_entry(uint32_t r0, uint32_t r1, uint32_t idx) {
+    const float inv8 = 1.0f / 1785.0f, inv6 = 1.0f / 1275.0f;
+    if (r0 > r1) {
+        uint32_t k = idx == 0 ? 0u : (idx == 1 ? 7u : idx - 1u);
+        return (float)((7u - k) * r0 + k * r1) * inv8;
+    }
+    if (idx == 6) return 0.0f;
+    if (idx == 7) return (float)1275u * inv6;
+    uint32_t k = idx == 0 ? 0u : (idx == 1 ? 5u : idx - 1u);
+    return (float)((5u - k) * r0 + k * r1) * inv6;
+}
+static float bc4_texel_value(uint64_t blk, int t) {
+    return bc4_entry((uint32_t)(blk & 255u), (uint32_t)((blk >> 8) & 255u), (uint32_t)((blk >> (16 + 3 * t)) & 7u));
+}
+
+// the 16 texel values of one BC4 block (format check against hand-computed palettes)
+void vro_bc4_decode_block(uint64_t block, float out[16]) {
+    for (int t = 0; t < 16; ++t) out[t] = bc4_texel_value(block, t);
+}
+
 static void load_slot(const vr_grid_view& v, oracle::Slot& d) {
     {
         d.valid = true;
@@ -2502,7 +2528,14 @@ static void load_slot(const vr_grid_view& v, oracle::Slot& d) {
         d.bounds.assign(v.brick_bounds, v.brick_bounds + (size_t)v.num_bricks * 4);
         d.data.resize((size_t)v.num_bricks * 1000);
         for (size_t i = 0; i < d.data.size(); ++i) {
-            if (v.brick_f32) d.data[i] = v.brick_f32[i];
+            if (v.brick_bc4) {
+                // brick b, apron voxel (x, y, z): block z * 9 + (y / 4) * 3 + x / 4 of the
+                // brick's 90, texel (y % 4) * 4 + x % 4
+                const size_t b = i / 1000;
+                const int r = (int)(i % 1000), x = r % 10, y = (r / 10) % 10, z = r / 100;
+                const uint64_t blk = v.brick_bc4[b * 90 + (size_t)(z * 9 + (y / 4) * 3 + x / 4)];
+                d.data[i] = bc4_texel_value(blk, (y % 4) * 4 + x % 4) * v.bc4_scale;
+            } else if (v.brick_f32) d.data[i] = v.brick_f32[i];
             else {
                 uint16_t hh = v.brick_f16[i];
                 uint32_t sign = ((uint32_t)hh & 0x8000u) << 16, e = (hh >> 10) & 0x1fu, mm = hh & 0x3ffu;

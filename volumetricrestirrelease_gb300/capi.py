@@ -16,6 +16,7 @@ VR_SAMPLER_HAMMERSLEY, VR_SAMPLER_R2 = 0, 1
 (VR_TRACK_RATIO, VR_TRACK_ANALYTIC, VR_TRACK_RAY_MARCHING, VR_TRACK_RESIDUAL_RATIO,
  VR_TRACK_ANALOG_RESIDUAL_RATIO) = range(5)
 VR_REPROJ_LINEAR, VR_REPROJ_NONE, VR_REPROJ_NO_BACKGROUND = range(3)
+VR_NUM_MAX_MIPS = 8
 VR_NUM_SLOTS = 16
 
 _i32, _u32, _f32 = C.c_int32, C.c_uint32, C.c_float
@@ -65,12 +66,14 @@ class GridView(C.Structure):
                 ("world_to_index", _f32 * 16), ("max_value", _f32), ("num_l1", _i32), ("num_bricks", _i32),
                 ("root_child", C.POINTER(_i32)), ("l1_vmin", C.POINTER(_i32)), ("l1_child", C.POINTER(_i32)),
                 ("brick_vmin", C.POINTER(_i32)), ("brick_bounds", C.POINTER(_f32)),
-                ("brick_f32", C.POINTER(_f32)), ("brick_f16", C.POINTER(C.c_uint16))]
+                ("brick_f32", C.POINTER(_f32)), ("brick_f16", C.POINTER(C.c_uint16)),
+                ("brick_bc4", C.POINTER(C.c_uint64)), ("bc4_scale", _f32)]
 
 
 class VolumeInfo(C.Structure):
     _fields_ = [("num_mips", _i32), ("res", _i32), ("voxel_size", _f32), ("supervoxel_diag", _f32),
-                ("num_bricks", _i32 * VR_NUM_SLOTS), ("device_bytes", C.c_int64), ("fp16", _i32), ("world_min", _f32 * 3)]
+                ("num_bricks", _i32 * VR_NUM_SLOTS), ("device_bytes", C.c_int64), ("fp16", _i32), ("world_min", _f32 * 3),
+                ("bc4", _i32)]
 
 
 class PointLight(C.Structure):
@@ -102,6 +105,7 @@ SIGNATURES = {
     "vr_set_emission": (_i32, [_P, _P, _f32, _f32, _f32, C.POINTER(_f32)]),
     "vr_volume_create_dense": (_i32, [C.POINTER(_f32), _i32, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
     "vr_volume_destroy": (None, [_P]),
+    "vr_volume_compress_bc4": (_i32, [_P]),
     "vr_volume_get_info": (_i32, [_P, C.POINTER(VolumeInfo)]),
     "vr_volume_get_slot": (_i32, [_P, _i32, C.POINTER(GridView)]),
     "vr_create": (_P, [C.POINTER(Options), _i32, _i32, C.POINTER(_i32)]),

@@ -718,6 +718,15 @@ int vr_volume_save_vbx(const vr_volume* v, const char* path) {
 }
 const char* vr_volume_vbx_error(void) { return g_vbxErr.c_str(); }
 void vr_volume_destroy(vr_volume* v) { delete v; }
+int vr_volume_compress_bc4(vr_volume* v) {
+    if (!v) return VR_ERR_INVALID_ARG;
+    for (int m = 0; m < v->v.num_mips && m < VR_NUM_MAX_MIPS; ++m) {
+        if (m > 0) vr::compress_slot_bc4(v->v.slots[m], false);
+        vr::compress_slot_bc4(v->v.slots[VR_NUM_MAX_MIPS + m], true);
+    }
+    v->v.bc4 = 1;
+    return VR_OK;
+}
 int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
     if (!v || !info) return VR_ERR_INVALID_ARG;
     memset(info, 0, sizeof(*info));
@@ -726,6 +735,7 @@ int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
     info->voxel_size = v->v.voxel_size;
     info->supervoxel_diag = v->v.supervoxel_diag;
     info->fp16 = v->v.fp16;
+    info->bc4 = v->v.bc4;
     for (int i = 0; i < 3; ++i) info->world_min[i] = v->v.world_min[i];
     int64_t bytes = 0;
     for (int s = 0; s < VR_NUM_SLOTS; ++s) {
@@ -734,7 +744,7 @@ int vr_volume_get_info(const vr_volume* v, vr_volume_info* info) {
         if (!g.valid) continue;
         bytes += (int64_t)g.root_child.size() * 4 + (int64_t)g.l1_vmin.size() * 4 + (int64_t)g.l1_child.size() * 4 +
                  (int64_t)g.brick_vmin.size() * 4 + (int64_t)g.brick_bounds.size() * 4 + (int64_t)g.brick_f32.size() * 4 +
-                 (int64_t)g.brick_f16.size() * 2;
+                 (int64_t)g.brick_f16.size() * 2 + (int64_t)g.brick_bc4.size() * 8;
     }
     info->device_bytes = bytes;
     return VR_OK;
@@ -874,8 +884,9 @@ int vr_set_emission(vr_context* c, const vr_volume* temp, float le_scale, float 
     d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
     d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
     if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
-    else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
-    if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) {
+    else if (!g.brick_f16.empty() || g.brick_bc4.empty()) d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+    else { d.bc4 = (const uint2*)up(g.brick_bc4.data(), g.brick_bc4.size() * 8); d.bc4Scale = g.bc4_scale; }
+    if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16 && !d.bc4)) {
         for (void* q : c->emisAllocs) cudaFree(q);
         c->emisAllocs.clear();
         memset(&c->scene.tslot, 0, sizeof(c->scene.tslot));
@@ -929,8 +940,9 @@ int vr_set_volume(vr_context* c, const vr_volume* vol, const vr_medium* m) {
         d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
         d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
         if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
-        else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
-        if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16)) {
+        else if (!g.brick_f16.empty() || g.brick_bc4.empty()) d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+        else { d.bc4 = (const uint2*)up(g.brick_bc4.data(), g.brick_bc4.size() * 8); d.bc4Scale = g.bc4_scale; }
+        if (!d.root || !d.l1vmin || !d.l1child || !d.bvmin || !d.bounds || (!d.f32 && !d.f16 && !d.bc4)) {
             for (void* q : c->sceneAllocs) cudaFree(q);
             c->sceneAllocs.clear();
             memset(c->scene.slots, 0, sizeof(vrd::DevSlot) * VR_NUM_SLOTS);
@@ -980,8 +992,9 @@ static bool upload_grid(const vr::GridSlot& g, vrd::DevSlot& d, std::vector<void
     d.bvmin = (const int4*)up(g.brick_vmin.data(), g.brick_vmin.size() * 4);
     d.bounds = (const float4*)up(g.brick_bounds.data(), g.brick_bounds.size() * 4);
     if (!g.brick_f32.empty()) d.f32 = (const float*)up(g.brick_f32.data(), g.brick_f32.size() * 4);
-    else d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
-    return d.root && d.l1vmin && d.l1child && d.bvmin && d.bounds && (d.f32 || d.f16);
+    else if (!g.brick_f16.empty() || g.brick_bc4.empty()) d.f16 = (const __half*)up(g.brick_f16.data(), g.brick_f16.size() * 2);
+    else { d.bc4 = (const uint2*)up(g.brick_bc4.data(), g.brick_bc4.size() * 8); d.bc4Scale = g.bc4_scale; }
+    return d.root && d.l1vmin && d.l1child && d.bvmin && d.bounds && (d.f32 || d.f16 || d.bc4);
 }
 
 static void anim_clear(vr_context* c) {

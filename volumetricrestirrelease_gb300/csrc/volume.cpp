@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "vr_math.h"
+#include "vr_bc4.h"
 
 namespace vr {
 
@@ -394,6 +395,104 @@ int build_volume(const std::vector<float>& dense, int R, int numMips, const floa
     return 0;
 }
 
+// ---------------------------------------------------------------------------------------
+// BC4 brick form (Scene.cpp:3161-3181, ATLAS_COMPRESSION 2).  The encoder is this project's
+// own: endpoints from the block's extremes (floor of the minimum, ceiling of the maximum, in
+// 1/255 steps), the six-value palette when the block holds an exact 0 or 1 (so those stay
+// exact, as the reference's encoder arranges) or when the extremes round to one code, the
+// eight-value palette otherwise; each texel takes the nearest palette entry.  For the
+// conservative grids a nonzero texel never takes a zero entry (the reference's
+// FindClosestUNORMConservative keeps nonzero texels nonzero, BCHelper.cpp:229-299), so distance
+// sampling on them still reaches every occupied voxel.  Padding texels (x or y of 10, 11) take
+// index 0 and do not take part in the endpoints.
+// ---------------------------------------------------------------------------------------
+float bc4_decode(uint64_t block, int texel) { return bc4_decode2((uint32_t)block, (uint32_t)(block >> 32), texel); }
+
+static uint64_t bc4_encode_block(const float u[16], const bool used[16], bool conservative) {
+    bool any = false, has0 = false, has1 = false, anyIn = false;
+    float lo = 1.0f, hi = 0.0f, loIn = 1.0f, hiIn = 0.0f;
+    for (int t = 0; t < 16; ++t) {
+        if (!used[t]) continue;
+        const float v = u[t];
+        any = true;
+        has0 |= v == 0.0f;
+        has1 |= v == 1.0f;
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+        if (v > 0.0f && v < 1.0f) { anyIn = true; loIn = std::min(loIn, v); hiIn = std::max(hiIn, v); }
+    }
+    auto code_lo = [](float v) { return (uint32_t)std::min(255.0f, std::floor(255.0f * v)); };
+    auto code_hi = [](float v) { return (uint32_t)std::min(255.0f, std::ceil(255.0f * v)); };
+    uint32_t r0 = 0, r1 = 0;
+    if (!any) {
+        r0 = r1 = 0;
+    } else if (has0 || has1) {
+        r0 = anyIn ? code_lo(loIn) : 0u;                 // r0 <= r1: six-value palette with 0 and 1
+        r1 = anyIn ? code_hi(hiIn) : 0u;
+    } else {
+        const uint32_t a = code_lo(lo), b = code_hi(hi);
+        if (b > a) { r0 = b; r1 = a; }                   // eight-value palette
+        else { r0 = r1 = a; }
+    }
+    uint64_t w = (uint64_t)r0 | ((uint64_t)r1 << 8);
+    float pal[8];
+    for (uint32_t i = 0; i < 8; ++i) pal[i] = bc4_palette(r0, r1, i);
+    for (int t = 0; t < 16; ++t) {
+        uint32_t best = 0;
+        if (used[t]) {
+            float bestD = FLT_MAX;
+            for (uint32_t i = 0; i < 8; ++i) {
+                if (conservative && u[t] > 0.0f && pal[i] == 0.0f) continue;
+                const float d = std::fabs(pal[i] - u[t]);
+                if (d < bestD) { bestD = d; best = i; }
+            }
+        }
+        w |= (uint64_t)best << (16 + 3 * t);
+    }
+    return w;
+}
+
+void compress_slot_bc4(GridSlot& s, bool conservative) {
+    if (!s.valid || !s.brick_bc4.empty()) return;
+    const int nb = s.num_bricks;
+    auto src = [&](size_t o) { return s.brick_f32.empty() ? half_to_float(s.brick_f16[o]) : s.brick_f32[o]; };
+    float scale = 0.0f;
+    for (size_t o = 0; o < (size_t)nb * 1000; ++o) scale = std::max(scale, src(o));
+    s.bc4_scale = scale;
+    s.brick_bc4.assign((size_t)nb * kBc4BlocksPerBrick, 0);
+    parallel_for(nb, [&](int b) {
+        const size_t base = (size_t)b * 1000;
+        for (int z = 0; z < 10; ++z)
+            for (int by = 0; by < 3; ++by)
+                for (int bx = 0; bx < 3; ++bx) {
+                    float u[16];
+                    bool used[16];
+                    for (int t = 0; t < 16; ++t) {
+                        const int x = bx * 4 + (t & 3), y = by * 4 + (t >> 2);
+                        used[t] = x < 10 && y < 10;
+                        const float v = used[t] ? src(base + (size_t)(z * 10 + y) * 10 + x) : 0.0f;
+                        u[t] = scale > 0.0f ? std::min(1.0f, std::max(0.0f, v / scale)) : 0.0f;
+                    }
+                    s.brick_bc4[(size_t)b * kBc4BlocksPerBrick + bc4_block(bx * 4, by * 4, z)] = bc4_encode_block(u, used, conservative);
+                }
+        // bounds of the decoded values over the same 10^3 box as build_slot, sum / 512
+        float mn = FLT_MAX, mx = 0.0f, sum = 0.0f;
+        for (int z = 0; z < 10; ++z)
+            for (int y = 0; y < 10; ++y)
+                for (int x = 0; x < 10; ++x) {
+                    const float v = bc4_decode(s.brick_bc4[(size_t)b * kBc4BlocksPerBrick + bc4_block(x, y, z)], bc4_texel(x, y)) * scale;
+                    mn = std::min(mn, v);
+                    mx = std::max(mx, v);
+                    sum += v;
+                }
+        s.brick_bounds[(size_t)b * 4 + 0] = mn;
+        s.brick_bounds[(size_t)b * 4 + 1] = mx;
+        s.brick_bounds[(size_t)b * 4 + 2] = sum / 512.0f;
+    });
+    s.brick_f32.clear(); s.brick_f32.shrink_to_fit();
+    s.brick_f16.clear(); s.brick_f16.shrink_to_fit();
+}
+
 void slot_view(const GridSlot& s, vr_grid_view* v) {
     memset(v, 0, sizeof(*v));
     v->valid = s.valid;
@@ -410,6 +509,8 @@ void slot_view(const GridSlot& s, vr_grid_view* v) {
     v->brick_bounds = s.brick_bounds.data();
     v->brick_f32 = s.brick_f32.empty() ? nullptr : s.brick_f32.data();
     v->brick_f16 = s.brick_f16.empty() ? nullptr : s.brick_f16.data();
+    v->brick_bc4 = s.brick_bc4.empty() ? nullptr : s.brick_bc4.data();
+    v->bc4_scale = s.bc4_scale;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "vr_math.h"
+#include "vr_bc4.h"
 #include "../../include/vrestir.h"
 
 namespace vrd {
@@ -53,6 +54,8 @@ struct DevSlot {
     const float4* bounds;
     const float* f32;            // 1000 per brick
     const __half* f16;
+    const uint2* bc4;            // 90 BC4 blocks per brick (vr_bc4.h), density = decoded * bc4Scale
+    float bc4Scale;
 };
 
 // slots [0, VR_NUM_SLOTS): the current frame's mips (normal, then conservative); with an
@@ -239,8 +242,14 @@ __device__ __forceinline__ f3 nodeVmin(const DevSlot& s, int lev, int id) {
     int4 v = lev == 1 ? __ldg(&s.l1vmin[id]) : __ldg(&s.bvmin[id]);
     return mk3((float)v.x, (float)v.y, (float)v.z);
 }
+// one voxel of a BC4 brick, apron coordinates in [0, 10)^3
+__device__ __forceinline__ float bc4Voxel(const DevSlot& s, int brick, int x, int y, int z) {
+    const uint2 b = __ldg(&s.bc4[(size_t)brick * vr::kBc4BlocksPerBrick + vr::bc4_block(x, y, z)]);
+    return vr::bc4_decode2(b.x, b.y, vr::bc4_texel(x, y)) * s.bc4Scale;
+}
 __device__ __forceinline__ float voxel(const DevSlot& s, int brick, int x, int y, int z) {
     x = min(max(x, -1), 8); y = min(max(y, -1), 8); z = min(max(z, -1), 8);
+    if (s.bc4) return bc4Voxel(s, brick, x + 1, y + 1, z + 1);
     size_t o = (size_t)brick * 1000 + ((z + 1) * 10 + (y + 1)) * 10 + (x + 1);
     if (s.f32) return __ldg(&s.f32[o]);
     return __half2float(__ldg(&s.f16[o]));
@@ -276,19 +285,43 @@ __device__ __forceinline__ void cornerValues(const DevSlot& s, size_t base, floa
         c[6] = __half2float(__ldg(d + 110)); c[7] = __half2float(__ldg(d + 111));
     }
 }
+// the eight corners from apron corner (x, y, z) in [0, 9)^3, in cornerValues' order
+__device__ __forceinline__ void cornerValuesAt(const DevSlot& s, int brick, int x, int y, int z, float c[8]) {
+    if (s.bc4) {
+        // the four corners of a z-slice share one block unless x or y is the last texel of its
+        // block: one load per slice, the others only where a corner crosses into the next block
+        const uint2* blk = s.bc4 + (size_t)brick * vr::kBc4BlocksPerBrick;
+        const bool cx = (x & 3) == 3, cy = (y & 3) == 3;
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz) {
+            const int zz = z + dz;
+            const uint2 b00 = __ldg(&blk[vr::bc4_block(x, y, zz)]);
+            const uint2 b10 = cx ? __ldg(&blk[vr::bc4_block(x + 1, y, zz)]) : b00;
+            const uint2 b01 = cy ? __ldg(&blk[vr::bc4_block(x, y + 1, zz)]) : b00;
+            const uint2 b11 = (cx || cy) ? __ldg(&blk[vr::bc4_block(x + 1, y + 1, zz)]) : b00;
+            c[4 * dz + 0] = vr::bc4_decode2(b00.x, b00.y, vr::bc4_texel(x, y)) * s.bc4Scale;
+            c[4 * dz + 1] = vr::bc4_decode2(b10.x, b10.y, vr::bc4_texel(x + 1, y)) * s.bc4Scale;
+            c[4 * dz + 2] = vr::bc4_decode2(b01.x, b01.y, vr::bc4_texel(x, y + 1)) * s.bc4Scale;
+            c[4 * dz + 3] = vr::bc4_decode2(b11.x, b11.y, vr::bc4_texel(x + 1, y + 1)) * s.bc4Scale;
+        }
+        return;
+    }
+    cornerValues(s, (size_t)brick * 1000 + (size_t)((z * 10 + y) * 10 + x), c);
+}
 __device__ __forceinline__ float trilinearIn(const DevSlot& s, int brick, f3 p) {
     float qx = p.x - 0.5f, qy = p.y - 0.5f, qz = p.z - 0.5f;
     float fx0 = vr::floor_(qx), fy0 = vr::floor_(qy), fz0 = vr::floor_(qz);
     int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
     float fx = qx - fx0, fy = qy - fy0, fz = qz - fz0;
     float c[8];
-    cornerValues(s, (size_t)brick * 1000 + (size_t)(((iz + 1) * 10 + (iy + 1)) * 10 + (ix + 1)), c);
+    cornerValuesAt(s, brick, ix + 1, iy + 1, iz + 1, c);
     float x00 = lerp_(c[0], c[1], fx), x10 = lerp_(c[2], c[3], fx);
     float x01 = lerp_(c[4], c[5], fx), x11 = lerp_(c[6], c[7], fx);
     float y0 = lerp_(x00, x10, fy), y1 = lerp_(x01, x11, fy);
     return lerp_(y0, y1, fz);
 }
 __device__ __forceinline__ float voxelIn(const DevSlot& s, int brick, int x, int y, int z) {
+    if (s.bc4) return bc4Voxel(s, brick, x + 1, y + 1, z + 1);
     size_t o = (size_t)brick * 1000 + (size_t)(((z + 1) * 10 + (y + 1)) * 10 + (x + 1));
     return s.f32 ? __ldg(&s.f32[o]) : __half2float(__ldg(&s.f16[o]));
 }
@@ -308,7 +341,7 @@ __device__ __forceinline__ float densityCell(int mip, int brick, const int p[3])
 }
 __device__ __forceinline__ void fetchEightSigma(int mip, int brick, const int p[3], float v[8]) {
     const DevSlot& s = c_scene.slots[mip];
-    cornerValues(s, (size_t)brick * 1000 + (size_t)(((p[2] + 1) * 10 + (p[1] + 1)) * 10 + (p[0] + 1)), v);
+    cornerValuesAt(s, brick, p[0] + 1, p[1] + 1, p[2] + 1, v);
 #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = v[i] * 1.0f * c_scene.dscale * c_scene.sigma_t;
 }

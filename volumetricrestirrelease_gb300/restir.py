@@ -90,6 +90,14 @@ class Volume:
             raise ValueError(f"vr_volume_create_dense failed ({r})")
         return cls(h, lib)
 
+    def compress_bc4(self):
+        """Re-encode the coarse normal mips and every conservative mip as BC4 blocks (the
+        reference's default texture form); normal mip 0 keeps its storage.  Returns self."""
+        r = self._lib.vr_volume_compress_bc4(self._h)
+        if r != capi.VR_OK:
+            raise ValueError(f"vr_volume_compress_bc4 failed ({r})")
+        return self
+
     def info(self):
         i = capi.VolumeInfo()
         self._lib.vr_volume_get_info(self._h, C.byref(i))
