@@ -50,12 +50,14 @@ def _samples(seed, n, box, invalid_frac=0.1):
     return s
 
 
-def _ctx(vlib, cuda, overrides=None, W=64, H=48):
+def _ctx(vlib, cuda, overrides=None, W=64, H=48, bc4=False):
     from oracle.oracle import Oracle
     from volumetricrestirrelease_gb300 import capi, scenes
     from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
     sc = scenes.small(width=W, height=H)
     vol = Volume.procedural(sc.volume, lib=vlib)
+    if bc4:
+        vol.compress_bc4()
     opts = capi.default_options(vlib)
     for k, v in {**sc.options, "mUseLearnedPHat": 1, "mLearnedTrainSamples": 2048, "mLearnedBatch": 512,
                  **(overrides or {})}.items():
@@ -137,10 +139,11 @@ def test_net_inference_tensor_cores(vlib, cuda):
     assert rel.max() < 5e-2
 
 
-def test_learned_frames_match_oracle(vlib, cuda):
+@pytest.mark.parametrize("bc4", [False, True], ids=["fp32", "bc4"])
+def test_learned_frames_match_oracle(vlib, cuda, bc4):
     from oracle.oracle import net_forward
     from volumetricrestirrelease_gb300.restir import as_reservoirs
-    sc, vol, opts, gpu, ora = _ctx(vlib, cuda)
+    sc, vol, opts, gpu, ora = _ctx(vlib, cuda, bc4=bc4)
     W, H = gpu.width, gpu.height
     out = cuda.empty((H, W, 4), device="cuda", dtype=cuda.float32)
     losses = []
