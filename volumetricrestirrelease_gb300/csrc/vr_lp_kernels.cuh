@@ -325,7 +325,14 @@ static __global__ void __launch_bounds__(256) k_path_scatter(const __grid_consta
     const float4* q = L.paths[b & 1];
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
         const float4 a = q[4 * i], c = q[4 * i + 1], d = q[4 * i + 2], e = q[4 * i + 3];
-        const int pos = atomicAdd(&L.hist[kPathKeys + lpPathKey(L, a, c)], 1);
+        // one cursor update per key and warp: the lanes holding the same key take consecutive
+        // places after the lowest of them reserved them all
+        const int key = lpPathKey(L, a, c);
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&L.hist[kPathKeys + key], __popc(peers));
+        const int pos = __shfl_sync(peers, base, leader) + __popc(peers & ((1u << lane) - 1u));
         if (pos < 0 || pos >= n) continue;                    // cannot happen: the cursors cover [0, n)
         float4* o = L.psort + 4 * (size_t)pos;
         o[0] = a; o[1] = c; o[2] = d; o[3] = e;
