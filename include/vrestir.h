@@ -330,6 +330,16 @@ int vr_render_frame_host(vr_context* ctx, const vr_camera* cam, float* out_rgba_
  * vr_host_frames_wait, or once the second call after its own has returned.  Bounded-loop errors
  * of the device are reported by vr_host_frames_wait. */
 int vr_render_frame_host_async(vr_context* ctx, const vr_camera* cam, float* out_rgba_host, void* stream);
+/* Post-process hook: the slot where the reference's graph puts its OptixDenoiser (and an
+ * AccumulatePass before it) after the pass (Scripts/run_plume_denoiser.py: accumulated_color ->
+ * AccumulatePass -> OptixDenoiser.color, mvec -> OptixDenoiser.mvec).  When set, every
+ * vr_render_frame* call invokes fn on the calling thread once the frame's last pass is enqueued,
+ * with the output image (RGBA32F, device), the motion vectors (RG32F, device) or NULL, the size
+ * and the frame's stream.  fn enqueues its work on that stream and may rewrite the image in place;
+ * the host copies of vr_render_frame_host* are enqueued after it.  NULL removes the hook. */
+typedef void (*vr_frame_hook)(void* user, float* rgba_device, float* mvec_device_or_null, int32_t width, int32_t height,
+                              void* stream);
+int vr_set_frame_hook(vr_context* ctx, vr_frame_hook fn, void* user);
 int vr_host_frames_wait(vr_context* ctx);
 
 /* ---- allocation-free frame (no counterpart in the reference) ----

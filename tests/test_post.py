@@ -115,3 +115,70 @@ def test_bad_arguments(vlib, cuda):
     p = C.c_void_p(x.data_ptr())
     assert vlib.vr_error_measure(p, p, None, 4, 4, 64, 0.0, err, None, None) != 0
     assert vlib.vr_error_measure(p, p, None, 4, 4, 8, -1.0, err, None, None) != 0
+
+
+def test_frame_hook_chain(vlib, cuda):
+    """vr_set_frame_hook in the slot of the reference graph's post chain (VolumetricReSTIR ->
+    AccumulatePass -> OptixDenoiser): a hook that accumulates each frame in place makes every
+    output, on the device and through the pipelined host path, the FP64 running mean of the
+    frames rendered without it, bit for bit; the hook sees the caller's motion-vector buffer and
+    the frame's stream, and removing it restores the plain output."""
+    from volumetricrestirrelease_gb300 import capi, scenes
+    from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
+    sc = scenes.small(width=64, height=48)
+    W, H = sc.width, sc.height
+    vol = Volume.procedural(sc.volume, lib=vlib)
+    opts = capi.default_options(vlib)
+    for k, v in sc.options.items():
+        setattr(opts, k, v)
+
+    def ctx():
+        r = VolumetricReSTIR(W, H, opts.as_dict(), lib=vlib)
+        r.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        return r
+    out = cuda.empty((H, W, 4), device="cuda", dtype=cuda.float32)
+    mvec = cuda.empty((H, W, 2), device="cuda", dtype=cuda.float32)
+    plain = ctx()
+    frames = []
+    for f in range(4):
+        plain.execute(sc.camera(f), out.data_ptr())
+        cuda.cuda.synchronize()
+        frames.append(out.cpu().numpy().astype(np.float64))
+    want = [(np.sum(frames[:k + 1], 0) / (k + 1)).astype(np.float32) for k in range(4)]
+
+    stream = cuda.cuda.current_stream().cuda_stream
+    for path in ("device", "host"):
+        acc = C.c_void_p()
+        assert vlib.vr_accumulator_create(W, H, 0, C.byref(acc)) == 0
+        calls = []
+
+        def hook(rgba, mv, w, h, st):
+            calls.append((rgba, mv, w, h, st))
+            assert vlib.vr_accumulate(acc, C.c_void_p(rgba), C.c_void_p(rgba), C.c_void_p(st)) == 0
+        r = ctx()
+        r.set_frame_hook(hook)
+        try:
+            if path == "device":
+                for f in range(3):
+                    r.execute(sc.camera(f), out.data_ptr(), mvec.data_ptr(), stream=stream)
+                    cuda.cuda.synchronize()
+                    got = out.cpu().numpy()
+                    assert np.array_equal(got.view(np.uint32), want[f].view(np.uint32)), f
+                assert all(c[0] == out.data_ptr() and c[1] == mvec.data_ptr() and c[2:4] == (W, H) and c[4] == stream for c in calls)
+            else:
+                hosts = [np.zeros((H, W, 4), np.float32) for _ in range(3)]
+                for f in range(3):
+                    assert vlib.vr_render_frame_host_async(r._h, C.byref(sc.camera(f)), hosts[f].ctypes.data_as(C.POINTER(C.c_float)),
+                                                           C.c_void_p(stream)) == 0
+                assert vlib.vr_host_frames_wait(r._h) == 0
+                for f in range(3):
+                    assert np.array_equal(hosts[f].view(np.uint32), want[f].view(np.uint32)), f
+                assert len(calls) == 3 and all(c[1] == 0 for c in calls)
+            # without the hook the next frame is the plain one
+            r.set_frame_hook(None)
+            r.execute(sc.camera(3), out.data_ptr(), stream=stream)
+            cuda.cuda.synchronize()
+            assert np.array_equal(out.cpu().numpy().view(np.uint32), frames[3].astype(np.float32).view(np.uint32))
+            assert len(calls) == 3
+        finally:
+            vlib.vr_accumulator_destroy(acc)

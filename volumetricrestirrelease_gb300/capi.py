@@ -76,6 +76,10 @@ class VolumeInfo(C.Structure):
                 ("bc4", _i32)]
 
 
+# void (*)(void* user, float* rgba, float* mvec, int32_t width, int32_t height, void* stream)
+FRAME_HOOK = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_void_p, _i32, _i32, C.c_void_p)
+
+
 class PointLight(C.Structure):
     _fields_ = [("pos", _f32 * 3), ("intensity", _f32 * 3)]
 
@@ -106,6 +110,7 @@ SIGNATURES = {
     "vr_volume_create_dense": (_i32, [C.POINTER(_f32), _i32, _i32, C.POINTER(_f32), _f32, _i32, C.POINTER(_P)]),
     "vr_volume_destroy": (None, [_P]),
     "vr_volume_compress_bc4": (_i32, [_P]),
+    "vr_set_frame_hook": (_i32, [_P, _P, _P]),
     "vr_volume_get_info": (_i32, [_P, C.POINTER(VolumeInfo)]),
     "vr_volume_get_slot": (_i32, [_P, _i32, C.POINTER(GridView)]),
     "vr_create": (_P, [C.POINTER(Options), _i32, _i32, C.POINTER(_i32)]),

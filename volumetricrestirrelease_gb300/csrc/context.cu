@@ -284,6 +284,8 @@ struct vr_context {
     int64_t h2d = 0, d2h = 0;
     int* status = nullptr;    // device status word
     int blockThreads = 128;   // pixel kernels: blocks of 8 x (blockThreads / 8) pixels
+    vr_frame_hook hook = nullptr;   // post-process hook (vr_set_frame_hook)
+    void* hookUser = nullptr;
     // the network trains on a side stream (non-blocking, so it also overlaps work on the legacy
     // default stream), forked after select and joined at the end of the frame
     cudaStream_t side = nullptr;
@@ -1261,6 +1263,17 @@ int vr_render_frame(vr_context* c, const vr_camera* cam, float* out_rgba, float*
     c->temporalSampleAccumulated = 1;
     c->prev = cf;
     c->frameCount++;
+    if (c->hook) {
+        c->hook(c->hookUser, out_rgba, out_mvec, c->W, c->H, stream);
+        if ((r = check_cuda(c, "frame hook"))) return r;
+    }
+    return VR_OK;
+}
+
+int vr_set_frame_hook(vr_context* c, vr_frame_hook fn, void* user) {
+    if (!c) return VR_ERR_INVALID_ARG;
+    c->hook = fn;
+    c->hookUser = fn ? user : nullptr;
     return VR_OK;
 }
 

@@ -239,6 +239,20 @@ class VolumetricReSTIR:
         self._check(self._lib.vr_render_frame(self._h, C.byref(camera), C.c_void_p(out_ptr),
                                               C.c_void_p(mvec_ptr) if mvec_ptr else None, C.c_void_p(stream)))
 
+    def set_frame_hook(self, fn):
+        """Post-process hook run after every frame (the slot of the reference graph's
+        OptixDenoiser): fn(rgba_ptr, mvec_ptr_or_0, width, height, stream) enqueues its work on
+        the frame's stream and may rewrite the image in place.  None removes it."""
+        if fn is None:
+            self._hook = None
+            self._check(self._lib.vr_set_frame_hook(self._h, None, None))
+            return
+
+        def call(user, rgba, mvec, w, h, stream):
+            fn(rgba or 0, mvec or 0, w, h, stream or 0)
+        self._hook = capi.FRAME_HOOK(call)            # kept alive with the context
+        self._check(self._lib.vr_set_frame_hook(self._h, C.cast(self._hook, C.c_void_p), None))
+
     def execute_host(self, camera, stream=0):
         out = np.empty((self.height, self.width, 4), np.float32)
         self._check(self._lib.vr_render_frame_host(self._h, C.byref(camera), out.ctypes.data_as(C.POINTER(C.c_float)),
