@@ -402,8 +402,10 @@ __device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameB
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
+// 4 blocks per SM (128 registers): the spills of the temporal evaluations drop from 188 to 88
+// bytes; measured 14.2 -> 13.7 ms per 1080p frame (3 blocks: 14.95 ms)
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
+__global__ void __launch_bounds__(128, 4) k_lp_select(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
