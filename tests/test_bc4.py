@@ -174,3 +174,39 @@ def test_bc4_frames_bit_exact(vlib, cuda, overrides):
     ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
     imgs = [_compare_frame(gpu, ora, opts, cuda, sc.camera(f), f) for f in range(3)]
     assert imgs[-1][..., :3].mean() > 0.02
+
+
+def test_oracle_renders_bc4_volumes(vlib, oracle_lib):
+    """The oracle's BC4 path on the CPU: frames on a BC4 volume are deterministic across thread
+    counts, finite, and close to the FP32 volume's frames (the coarse and conservative mips only
+    steer sampling and the reuse targets; the shading reads mip 0)."""
+    from oracle.oracle import Oracle
+    from volumetricrestirrelease_gb300 import capi, scenes
+    from volumetricrestirrelease_gb300.restir import Volume
+    sc = scenes.small(width=32, height=24)
+    opts = capi.default_options(vlib)
+    for k, v in sc.options.items():
+        setattr(opts, k, v)
+    means = {}
+    for form in ("fp32", "bc4"):
+        vol = Volume.procedural(sc.volume, lib=vlib)
+        if form == "bc4":
+            vol.compress_bc4()
+        imgs = []
+        for threads in (1, 3):
+            ora = Oracle(sc.width, sc.height, opts, threads=threads)
+            ora.set_volume(vol, sc.medium)
+            ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
+            for f in range(3):
+                img = ora.render_frame(sc.camera(f))
+            imgs.append(img)
+        assert np.array_equal(imgs[0].view(np.uint32), imgs[1].view(np.uint32))
+        assert np.isfinite(imgs[0]).all()
+        means[form] = float(imgs[0][..., :3].mean())
+    assert means["fp32"] > 0.02
+    assert abs(means["bc4"] - means["fp32"]) < 0.1 * means["fp32"], means
+
+
+def test_bad_arguments(vlib):
+    assert vlib.vr_volume_compress_bc4(None) != 0
+    assert vlib.vr_set_frame_hook(None, None, None) != 0
