@@ -336,7 +336,8 @@ int vr_render_frame_host_async(vr_context* ctx, const vr_camera* cam, float* out
  * vr_render_frame* call invokes fn on the calling thread once the frame's last pass is enqueued,
  * with the output image (RGBA32F, device), the motion vectors (RG32F, device) or NULL, the size
  * and the frame's stream.  fn enqueues its work on that stream and may rewrite the image in place;
- * the host copies of vr_render_frame_host* are enqueued after it.  NULL removes the hook. */
+ * the host copies of vr_render_frame_host* are enqueued after it.  NULL removes the hook.
+ * Batched rendering (vr_batch_*) does not call it. */
 typedef void (*vr_frame_hook)(void* user, float* rgba_device, float* mvec_device_or_null, int32_t width, int32_t height,
                               void* stream);
 int vr_set_frame_hook(vr_context* ctx, vr_frame_hook fn, void* user);
