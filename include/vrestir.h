@@ -347,13 +347,15 @@ int vr_host_frames_wait(vr_context* ctx);
  * Renders one frame without temporal history into out_rgba_device, keeping every per-pixel
  * intermediate in a fixed static device array (about 6.3 MiB, held by each GPU that loads the
  * library until exit) instead of allocating.  For callers that may not allocate GPU memory at
- * render time: fixed-budget hosts, real-time loops where cudaMalloc would stall, code running
- * under stream capture.  Limits: at most 65536 pixels, mMaxBounces <= 2, mEnableTemporalReuse
- * and mUseReference off; larger requests fail with VR_ERR_INVALID_ARG.  frame_index seeds the
- * per-pixel RNG like the frame counter.  Calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller.  The first call on each device looks up the
- * array's address; make it before any stream capture.  Context buffers, counters and history
- * are left untouched. */
+ * render time: hosts that hand out a fixed device-memory budget up front and forbid later
+ * allocations, and real-time loops where a cudaMalloc (which can synchronise the device) would
+ * stall a frame.  Limits: at most 65536 pixels, mMaxBounces <= 2, mEnableTemporalReuse,
+ * mUseReference and mUseLearnedPHat off; other requests fail with VR_ERR_INVALID_ARG.
+ * frame_index seeds the per-pixel RNG and the neighbour offsets like the frame counter.  Calls
+ * share the array and the scene constants of the entry point's own kernels, which every call
+ * rewrites: calls that overlap on the GPU race and must be serialised by the caller.  The first
+ * call on each device looks up the array's address; make it before any stream capture.
+ * Context buffers, counters and history are left untouched. */
 int vr_render_frame_noalloc(vr_context* ctx, const vr_camera* cam, int32_t frame_index,
                             float* out_rgba_device, void* stream);
 

@@ -1944,6 +1944,12 @@ int noalloc_prepare(vr_context* c, const vr_camera* cam, int32_t frame_index, No
         return VR_ERR_INVALID_ARG;
     }
     if (o.mMaxBounces > kNoAllocMaxBounces) { c->err = "vr_render_frame_noalloc supports mMaxBounces <= 2"; return VR_ERR_INVALID_ARG; }
+    if (lp_active(c)) {
+        // the learned target needs its vertex records, queries and network buffers, which this
+        // entry point has no room for: refuse rather than render the plain form silently
+        c->err = "vr_render_frame_noalloc renders the plain target only: disable mUseLearnedPHat";
+        return VR_ERR_INVALID_ARG;
+    }
     if ((int64_t)c->W * c->H > kNoAllocMaxPixels) {
         c->err = "vr_render_frame_noalloc supports at most 65536 pixels (e.g. 256x256); its scratch is a fixed static buffer";
         return VR_ERR_INVALID_ARG;

@@ -3,19 +3,21 @@
 // fixed static device array instead of buffers the library allocates.
 //
 // Who needs it: callers that must not allocate GPU memory at render time -- hosts that hand
-// out a fixed memory budget up front and forbid later allocations, real-time loops where a
-// cudaMalloc (which can synchronise the device) would stall a frame, and code that runs while
-// a stream is being captured.  The scene (volume, lights) must already be bound to the
-// context, which is done once at set-up.
+// out a fixed memory budget up front and forbid later allocations (an engine or plugin host
+// that owns the device heap), and real-time loops where a cudaMalloc, which can synchronise
+// the whole device, would stall a frame.  The scene (volume, lights) must already be bound to
+// the context, which is done once at set-up.
 //
 // Limits and behaviour:
-//   * at most 65536 pixels (for example 256 x 256) and max path length 2; temporal reuse and
-//     the reference mode must be off (there is no history to keep between calls);
+//   * at most 65536 pixels (for example 256 x 256) and max path length 2; temporal reuse,
+//     the reference mode and the learned target must be off (there is no history to keep
+//     between calls and no room for the learned target's records);
 //   * the scratch array is about 6.3 MiB and every GPU that loads the library holds it until
 //     the process exits;
 //   * every call on a device shares the one array and it keeps the last call's contents, so
 //     each call clears the part it reads before writing; calls whose work overlaps on the GPU
-//     (two streams, two host threads) race on it and must be serialised by the caller;
+//     (two streams, two host threads) race on it and must be serialised by the caller; they
+//     also share this file's copy of the scene constants, which each call rewrites;
 //   * the first call on each device looks up the array's device address (cudaGetSymbolAddress,
 //     with that device current); make that first call before any stream capture.
 #include <cuda_runtime.h>
@@ -99,8 +101,9 @@ extern "C" int vr_render_frame_noalloc(vr_context* ctx, const vr_camera* cam, in
     B.mvec = nullptr;
     // the array keeps the previous call's data: clear what this frame may read before writing
     // (the spatial buffer's suffix plane is read for pixels that keep their own reservoir)
-    cudaMemsetAsync(B.sp[1].extra, 0, N * 16, st);
-    cudaMemsetAsync(B.cur.extra, 0, N * 16, st);
+    e = cudaMemsetAsync(B.sp[1].extra, 0, N * 16, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.cur.extra, 0, N * 16, st);
+    if (e != cudaSuccess) { vrk::noalloc_error(ctx, "vr_render_frame_noalloc: clearing the scratch array failed"); return VR_ERR_CUDA; }
     e = cudaMemcpyToSymbolAsync(vrd::c_scene, f.scene, sizeof(vrd::DevScene), 0, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { vrk::noalloc_error(ctx, "vr_render_frame_noalloc: scene upload failed"); return VR_ERR_CUDA; }
     if (f.maxBounces == 1) launch<1>(f, B, st);
