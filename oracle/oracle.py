@@ -46,6 +46,10 @@ def _load():
         "vro_export_lp": (C.c_int64, [P, C.c_int, P, C.c_int64]),
         "vro_net_forward": (None, [P, P, P, C.c_float, P, C.c_int, P]),
         "vro_net_gradients": (None, [P, P, P, P, C.c_int, C.c_int, C.c_float, P, P]),
+        "vro_volume_procedural": (P, [P]),
+        "vro_volume_info": (C.c_int, [P, P]),
+        "vro_volume_slot": (C.c_int, [P, C.c_int, P]),
+        "vro_volume_destroy": (None, [P]),
     }
     for k, (r, a) in sig.items():
         f = getattr(lib, k)
@@ -66,6 +70,41 @@ def lib():
 
 def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleVolume:
+    """A procedural input grid built by the oracle's library (no GPU library involved), with the
+    views()/info()/slot() interface of restir.Volume that Oracle.set_volume reads."""
+
+    def __init__(self, desc):
+        self.L = lib()
+        self._h = self.L.vro_volume_procedural(C.byref(desc))
+        if not self._h:
+            raise ValueError("vro_volume_procedural failed")
+
+    def info(self):
+        from volumetricrestirrelease_gb300 import capi
+        i = capi.VolumeInfo()
+        self.L.vro_volume_info(self._h, C.byref(i))
+        return i
+
+    def slot(self, s):
+        from volumetricrestirrelease_gb300 import capi
+        v = capi.GridView()
+        self.L.vro_volume_slot(self._h, s, C.byref(v))
+        return v
+
+    def views(self):
+        from volumetricrestirrelease_gb300 import capi
+        arr = (capi.GridView * capi.VR_NUM_SLOTS)()
+        for s in range(capi.VR_NUM_SLOTS):
+            self.L.vro_volume_slot(self._h, s, C.byref(arr[s]))
+        return arr
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self.L.vro_volume_destroy(self._h)
+            self._h = None
 
 
 class Oracle:
@@ -211,6 +250,111 @@ class Oracle:
         if getattr(self, "_h", None):
             self.L.vro_destroy(self._h)
             self._h = None
+
+
+# VolumetricReSTIRParams defaults (VolumetricReSTIR.h:130-207) and the learned target's, so that
+# CPU-only runs fill a vr_options without the GPU library (a test checks them against
+# vr_options_default)
+OPTION_DEFAULTS = dict(
+    mMaxBounces=1, mEnableTemporalReuse=1, mEnableSpatialReuse=1, mUseReference=0, mUseEnvironmentLights=1,
+    mUseAnalyticLights=0, mBaselineSamplePerPixel=1, mVisualizeTotalTransmittance=0, mInitialBaseMipLevel=1,
+    mInitialM=4, mInitialLightSamples=1, mInitialLightingMipLevel=2, mInitialVisibilityUseLinearSampler=0,
+    mInitialLightingUseLinearSampler=1, mInitialLightingTrackingMethod=2, mInitialVisibilityTStepScale=1.0,
+    mInitialLightingTStepScale=2.0, mInitialUseRussianRoulette=1, mInitialUseCoarserGridForIndirectBounce=1,
+    mTemporalReuseMThreshold=4.0, mTemporalReprojectionMode=0, mTemporalMISMethod=1, mTemporalReprojectionMipLevel=1,
+    mSpatialReuseRounds=1, mSpatialVisibilityMipLevel=1, mSpatialLightingMipLevel=1, mSpatialVisibilityUseLinearSampler=1,
+    mSpatialLightingUseLinearSampler=1, mSpatialVisibilityTStepScale=1.0, mSpatialLightingTStepScale=1.0,
+    mSpatialVisibilityTrackingMethod=2, mSpatialLightingTrackingMethod=2, mRandomSamplerType=1, mSampleRadius=10.0,
+    mSpatialSampleCount=4, mSpatialMISMethod=1, mFinalLightSamples=1, mFinalVisibilitySamples=1,
+    mFinalVisibilityTrackingMethod=1, mFinalLightTrackingMethod=1, mFinalTStepScale=0.2, mUseLearnedPHat=0,
+    mLearnedTrainSamples=1 << 20, mLearnedBatch=16384, mLearnedLearningRate=1e-3, mLearnedTFloor=0.02, mLearnedSeed=1,
+    mLearnedTargetMethod=2, mLearnedLoss=0, mUsePrevVolumeForReproj=1)
+
+
+def default_options(**overrides):
+    from volumetricrestirrelease_gb300 import capi
+    o = capi.Options()
+    for k, v in {**OPTION_DEFAULTS, **overrides}.items():
+        setattr(o, k, v)
+    return o
+
+
+NET_PARAMS = 16705
+
+
+def _splitmix64(state):
+    state = (state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = state
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return state, z ^ (z >> 31)
+
+
+def net_init(seed):
+    """The learned target's initial weights for a seed: He-uniform hidden matrices from a
+    SplitMix64 stream, small output weights (T starts near 1), zero biases, layer 0's four pad
+    columns zero."""
+    w = np.zeros(NET_PARAMS, np.float32)
+    st = (0x6C7E3A91D2B54F08 ^ (seed << 17)) & 0xFFFFFFFFFFFFFFFF
+
+    def uni():
+        nonlocal st
+        st, z = _splitmix64(st)
+        return np.float32(np.float32((z >> 40) * (1.0 / 16777216.0)) * np.float32(2.0) - np.float32(1.0))
+    for l in range(4):
+        bound = np.float32(np.sqrt(np.float32(6.0) / np.float32(60 if l == 0 else 64)))
+        base = l * (4096 + 64)
+        for r in range(64):
+            for k in range(64):
+                u = uni()
+                w[base + r * 64 + k] = 0.0 if (l == 0 and k >= 60) else u * bound
+    ob = np.float32(np.float32(0.1) * np.sqrt(np.float32(6.0) / np.float32(64)))
+    for k in range(64):
+        w[4 * (4096 + 64) + k] = uni() * ob
+    return w
+
+
+class CpuTrainer:
+    """Adam on the transmittance network with the oracle's gradient (BF16 operands, FP32 sums),
+    the batch split over host threads (each chunk's mean gradient, averaged in chunk order)."""
+
+    def __init__(self, params, box, lr=1e-3, threads=0, loss_log=0, floor=0.02):
+        import os
+        self.w = np.ascontiguousarray(params, np.float32).copy()
+        self.m = np.zeros_like(self.w)
+        self.v = np.zeros_like(self.w)
+        self.t = 0
+        self.lr = lr
+        self.box = [np.ascontiguousarray(b, np.float32) for b in box]
+        self.threads = threads or os.cpu_count() or 1
+        self.loss_log, self.floor = loss_log, floor
+
+    def step(self, samples):
+        import concurrent.futures as cf
+        s = np.ascontiguousarray(samples, np.float32).reshape(-1, 8)
+        parts = np.array_split(np.arange(len(s)), self.threads)
+        parts = [p for p in parts if len(p)]
+        L = lib()
+        grads = [np.zeros(NET_PARAMS, np.float32) for _ in parts]
+        losses = [np.zeros(1, np.float32) for _ in parts]
+        chunks = [np.ascontiguousarray(s[p[0]:p[-1] + 1]) for p in parts]
+
+        def run(i):
+            L.vro_net_gradients(_ptr(self.w), _ptr(self.box[0]), _ptr(self.box[1]), _ptr(chunks[i]), len(chunks[i]),
+                                int(self.loss_log), float(self.floor), _ptr(grads[i]), _ptr(losses[i]))
+        with cf.ThreadPoolExecutor(len(parts)) as ex:
+            list(ex.map(run, range(len(parts))))
+        g = np.zeros(NET_PARAMS, np.float64)
+        for gi, p in zip(grads, parts):
+            g += gi.astype(np.float64) * (len(p) / len(s))
+        g = g.astype(np.float32)
+        self.t += 1
+        self.m = np.float32(0.9) * self.m + np.float32(0.1) * g
+        self.v = np.float32(0.999) * self.v + np.float32(0.001) * g * g
+        c1 = np.float32(1.0 - 0.9 ** self.t)
+        c2 = np.float32(1.0 - 0.999 ** self.t)
+        self.w = (self.w - np.float32(self.lr) * (self.m / c1) / (np.sqrt(self.v / c2) + np.float32(1e-8))).astype(np.float32)
+        return float(sum(float(l[0]) * len(p) for l, p in zip(losses, parts)) / len(s))
 
 
 def voxel_reads():

@@ -1311,23 +1311,45 @@ static void features(const float x[3], const float w[3], const float bmin[3], co
     for (int k = kIn; k < kInPad; ++k) f[k] = 0.f;
 }
 
-// forward pass keeping the BF16 activations of every layer (act[0] = encoded input)
-static float forward(const float* P, const float x[3], const float w[3], const float bmin[3], const float binv[3], float act[5][64]) {
+// The weight matrices rounded to BF16 once, stored input-major ([layer][k][n], then the 64
+// output weights), so that a layer's 64 outputs accumulate side by side; each output is still
+// summed over k in index order, so the values are those of the row-by-row form.
+static void roundedWeights(const float* P, std::vector<float>& wt) {
+    wt.assign((size_t)kLayers * 4096 + 64, 0.f);
+    for (int l = 0; l < kLayers; ++l)
+        for (int n = 0; n < kHid; ++n)
+            for (int k = 0; k < kInPad; ++k) wt[(size_t)l * 4096 + (size_t)k * 64 + n] = rb(P[l * kLayerStride + n * 64 + k]);
+    for (int k = 0; k < kHid; ++k) wt[(size_t)kLayers * 4096 + k] = rb(P[kOutW + k]);
+}
+
+// forward pass keeping the BF16 activations of every layer (act[0] = encoded input); wt from
+// roundedWeights(P)
+static float forwardR(const float* P, const float* wt, const float x[3], const float w[3], const float bmin[3], const float binv[3],
+                      float act[5][64]) {
     float f[kInPad];
     features(x, w, bmin, binv, f);
     for (int k = 0; k < kInPad; ++k) act[0][k] = rb(f[k]);
     for (int l = 0; l < kLayers; ++l) {
-        const float* W = P + l * kLayerStride;
+        const float* Wl = wt + (size_t)l * 4096;
+        float acc[kHid];
+        for (int n = 0; n < kHid; ++n) acc[n] = 0.f;
+        for (int k = 0; k < kInPad; ++k) {
+            const float a = act[l][k];
+            for (int n = 0; n < kHid; ++n) acc[n] += Wl[k * 64 + n] * a;
+        }
         for (int n = 0; n < kHid; ++n) {
-            float acc = 0.f;
-            for (int k = 0; k < kInPad; ++k) acc += rb(W[n * 64 + k]) * act[l][k];
-            float a = acc + W[4096 + n];
-            act[l + 1][n] = rb(a > 0.f ? a : 0.f);
+            float z = acc[n] + P[l * kLayerStride + 4096 + n];
+            act[l + 1][n] = rb(z > 0.f ? z : 0.f);
         }
     }
     float o = 0.f;
-    for (int k = 0; k < kHid; ++k) o += act[4][k] * rb(P[kOutW + k]);
+    for (int k = 0; k < kHid; ++k) o += act[4][k] * wt[(size_t)kLayers * 4096 + k];
     return o + P[kOutB];
+}
+static float forward(const float* P, const float x[3], const float w[3], const float bmin[3], const float binv[3], float act[5][64]) {
+    std::vector<float> wt;
+    roundedWeights(P, wt);
+    return forwardR(P, wt.data(), x, w, bmin, binv, act);
 }
 static float predict(float o, float floor_) {
     float t = exp_(o);
@@ -1341,6 +1363,9 @@ static float predict(float o, float floor_) {
 static void gradients(const float* P, const float* samples, int n, const float bmin[3], const float binv[3], int lossLog, float floor_,
                       float* grad, float* loss) {
     const float invB = 1.f / (float)n;
+    std::vector<float> wt, Pr(kParams);
+    roundedWeights(P, wt);
+    for (int i = 0; i < kParams; ++i) Pr[i] = rb(P[i]);      // only the weight entries are read rounded
     std::vector<float> tot(kParams, 0.f), part(kParams);
     float lossTot = 0.f;
     std::vector<float> act((size_t)128 * 5 * 64), g(128), lv(128), dzs((size_t)128 * 64), dhs((size_t)128 * 64);
@@ -1358,18 +1383,18 @@ static void gradients(const float* P, const float* samples, int n, const float b
                 valid = q[6] >= 0.f;
             }
             float o;
-            if (si < n) o = forward(P, x, w, bmin, binv, a);
+            if (si < n) o = forwardR(P, wt.data(), x, w, bmin, binv, a);
             else {
                 for (int k = 0; k < 64; ++k) a[0][k] = 0.f;
                 for (int l = 0; l < kLayers; ++l)
                     for (int m = 0; m < kHid; ++m) {
                         float acc = 0.f;
-                        for (int k = 0; k < kInPad; ++k) acc += rb(P[l * kLayerStride + m * 64 + k]) * a[l][k];
+                        for (int k = 0; k < kInPad; ++k) acc += Pr[l * kLayerStride + m * 64 + k] * a[l][k];
                         float z = acc + P[l * kLayerStride + 4096 + m];
                         a[l + 1][m] = rb(z > 0.f ? z : 0.f);
                     }
                 o = 0.f;
-                for (int k = 0; k < kHid; ++k) o += a[4][k] * rb(P[kOutW + k]);
+                for (int k = 0; k < kHid; ++k) o += a[4][k] * Pr[kOutW + k];
                 o += P[kOutB];
             }
             (void)o;
@@ -1386,7 +1411,7 @@ static void gradients(const float* P, const float* samples, int n, const float b
                     lv[t] = d * d * invB;
                 }
             }
-            for (int k = 0; k < kHid; ++k) dhs[(size_t)t * 64 + k] = g[t] * rb(P[kOutW + k]);
+            for (int k = 0; k < kHid; ++k) dhs[(size_t)t * 64 + k] = g[t] * Pr[kOutW + k];
         }
         for (int k = 0; k < kHid; ++k) {
             float acc = 0.f;
@@ -1400,7 +1425,7 @@ static void gradients(const float* P, const float* samples, int n, const float b
             lossTot += ls;
         }
         for (int l = kLayers - 1; l >= 0; --l) {
-            const float* W = P + l * kLayerStride;
+            const float* W = Pr.data() + l * kLayerStride;
             for (int t = 0; t < 128; ++t) {
                 float* dz = &dzs[(size_t)t * 64];
                 float* dh = &dhs[(size_t)t * 64];
@@ -1409,7 +1434,7 @@ static void gradients(const float* P, const float* samples, int n, const float b
                 if (l > 0)
                     for (int k = 0; k < kHid; ++k) {
                         float acc = 0.f;
-                        for (int m = 0; m < kHid; ++m) acc += rb(W[m * 64 + k]) * dz[m];
+                        for (int m = 0; m < kHid; ++m) acc += W[m * 64 + k] * dz[m];
                         dh[k] = acc;
                     }
             }
@@ -1940,6 +1965,8 @@ struct Oracle {
         lpQueries.assign((size_t)M * mb * N * 8, 0.f);
         lpTUsed.assign((size_t)M * mb * N, 0.f);
         const bool haveT = lpTIn.size() == (size_t)M * mb * N;
+        std::vector<float> lpWt;
+        if (!haveT) lpo::roundedWeights(lpParams.data(), lpWt);
         std::atomic<bool> ll(false);
         lpVertices = 0;
         forRows([&](int y) {
@@ -1972,7 +1999,7 @@ struct Oracle {
                                 if (haveT) t = lpTIn[slot];
                                 else {
                                     float act[5][64];
-                                    float o = lpo::forward(lpParams.data(), &q[b * 8], &q[b * 8 + 3], lpBmin, lpBinv, act);
+                                    float o = lpo::forwardR(lpParams.data(), lpWt.data(), &q[b * 8], &q[b * 8 + 3], lpBmin, lpBinv, act);
                                     t = lpo::predict(o, opts.mLearnedTFloor);
                                 }
                                 lpTUsed[slot] = t;
@@ -2791,9 +2818,11 @@ int64_t vro_export_lp(void* h, int which, float* out, int64_t cap) {
     return (int64_t)v.size();
 }
 void vro_net_forward(const float* params, const float bmin[3], const float binv[3], float floor_, const float* q, int n, float* out) {
+    std::vector<float> wt;
+    oracle::lpo::roundedWeights(params, wt);
     for (int i = 0; i < n; ++i) {
         float act[5][64];
-        float o = oracle::lpo::forward(params, q + (size_t)i * 8, q + (size_t)i * 8 + 3, bmin, binv, act);
+        float o = oracle::lpo::forwardR(params, wt.data(), q + (size_t)i * 8, q + (size_t)i * 8 + 3, bmin, binv, act);
         out[i] = oracle::lpo::predict(o, floor_);
     }
 }
