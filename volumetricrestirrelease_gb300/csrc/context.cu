@@ -482,7 +482,7 @@ static int lp_alloc(vr_context* c) {
         c->lp.paths[0] = dalloc<float4>(MB > 2 ? 4 * paths : 4);
         c->lp.psort = dalloc<float4>(4 * paths);
         c->lp.hist = dalloc<int>(2 * vrd::kPathKeys);
-        c->lp.pcount = dalloc<int>(MB + 1);
+        c->lp.pcount = dalloc<int>(16);         // queue lengths [0, MB], walk cursors from 8 on
         if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train ||
             !c->lp.paths[0] || !c->lp.paths[1] || !c->lp.pcount || !c->lp.psort || !c->lp.hist) {
             free_lp(c);
@@ -491,7 +491,8 @@ static int lp_alloc(vr_context* c) {
         }
         cudaMemset(c->lp.T, 0, slots * sizeof(float));
         cudaMemset(c->lp.qcount, 0, sizeof(int));
-        cudaMemset(c->lp.pcount, 0, (MB + 1) * sizeof(int));
+        cudaMemset(c->lp.pcount, 0, 16 * sizeof(int));
+        c->lp.wcursor = c->lp.pcount + 8;
         c->lp.qcapacity = (int)slots;
         c->lp.pcapacity = (int)paths;
         c->lp.numSlots = M * MB;
@@ -1708,12 +1709,12 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
     const bool lpOn = lp_active(c);
     if (lpOn) {
         cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
-        cudaMemsetAsync(c->lp.pcount, 0, (MB + 1) * sizeof(int), st);
+        cudaMemsetAsync(c->lp.pcount, 0, 16 * sizeof(int), st);
         for (int k = 0; k < 3; ++k) { c->lp.kmin[k] = c->netBmin[k]; c->lp.kinv[k] = c->netBinv[k]; }
         VR_RANGE("vr.generate");
         launch_lp_generate<MB>(P, B, c->lp, grid, block, st);
         for (int b = 1; b < MB; ++b) launch_lp_bounce<MB>(P, c->lp, b, c->numSMs * VR_KINIT_MIN_BLOCKS, st);
-        c->launches += 4 * (MB - 1);
+        c->launches += (P.initial.visibilityUseLinearSampler ? 4 : 5) * (MB - 1);
         VR_RANGE_END();
         rec();
         VR_RANGE("vr.infer");
@@ -2192,7 +2193,7 @@ static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
         for (vr_context* c : b->ctx)
             if (lp_active(c)) {
                 cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
-                cudaMemsetAsync(c->lp.pcount, 0, (MB + 1) * sizeof(int), st);
+                cudaMemsetAsync(c->lp.pcount, 0, 16 * sizeof(int), st);
             }
         batch_pass<MB>(BL, 1, grid, st);
         launches++;

@@ -39,7 +39,13 @@ void VR_CAT(launch_lp_select_, VR_MB)(const vrd::FrameParams& P, const vrd::Fram
     vrd::k_lp_select<VR_MB><<<g, b, 0, st>>>(P, B, L);
 }
 void VR_CAT(launch_lp_bounce_, VR_MB)(const vrd::FrameParams& P, const vrd::LpBuffers& L, int b, int grid, int sorted, cudaStream_t st) {
-    vrd::k_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(P, L, b, sorted);
+    // point-sampled distances of a sorted queue: the resumable walks, then the vertices
+    if (sorted && !P.initial.visibilityUseLinearSampler) {
+        vrd::k_lp_walk<VR_MB><<<grid, 128, 0, st>>>(P, L, b);
+        vrd::k_lp_vertex<VR_MB><<<grid, 128, 0, st>>>(P, L, b);
+    } else {
+        vrd::k_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(P, L, b, sorted);
+    }
 }
 // counting sort of the queue of bounce b into L.psort
 void VR_CAT(launch_lp_sort_, VR_MB)(const vrd::LpBuffers& L, int b, int grid, cudaStream_t st) {

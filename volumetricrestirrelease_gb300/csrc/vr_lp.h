@@ -49,6 +49,7 @@ struct LpBuffers {
     uint4* rng;        // [N]: the pixel's random state after generation
     float4* paths[2];  // queues of continuing candidate paths, 4 float4 each (the bounce b queue is paths[b & 1])
     int* pcount;       // [MB]: queue lengths by bounce
+    int* wcursor;      // [MB]: next entry of each queue for the resumable walks (k_lp_walk)
     int pcapacity;     // entries of each queue (M * N)
     float4* psort;     // a queue sorted by coherence key before its bounce pass (single-context frames)
     int* hist;         // [2][kPathKeys]: key counts, then scatter cursors

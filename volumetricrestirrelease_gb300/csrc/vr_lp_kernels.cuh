@@ -273,6 +273,218 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_bounce(const __
         lpBouncePath<MB>(P, L, b, src, i);
 }
 
+// ---------------------------------------------------------------------------------------
+// The bounce pass in two kernels: k_lp_walk samples the distance of every queued path, and
+// k_lp_vertex then builds the vertices.  k_lp_walk keeps the walk of trackVolume + SampleDist
+// (one sample, point-sampled) as explicit per-lane state and advances it one step per loop
+// trip, a step being one node of the tree or one voxel of a brick; a lane whose walk ends
+// stores its result and takes the next path of the queue (warp-aggregated counter) while the
+// other lanes of its warp go on walking, so the lanes of a warp stay on live walks instead of
+// waiting for the longest walk of the warp.  Every walk performs the operations of
+// trackVolume(..., SampleDist) in the same order, so results are bit-identical.  The result
+// goes back into the queue entry: pathPdf * pdf, pathPHat * Tr (the first operations of
+// lpVertex on either value), the hit distance and the random state after the walk.
+// ---------------------------------------------------------------------------------------
+struct LpWalk {
+    HDDA dda, dl;               // node-level walk, brick-level walk (dl = dda prepared for the leaf)
+    float tFar, t, thick;
+    float tMax1, tMax2;         // exits of the level-1 and root nodes
+    f3 vmin;                    // origin of the current node
+    int lev, node, nid1, brick; // level, current node, level-1 node, brick being walked
+    int oiter, biter;           // trip counters of trackVolume's node loop and the brick loop
+    float hit, tr, pdf;
+    vr::Rng g;
+    size_t entry;
+    bool inBrick;
+};
+
+// trackVolume's climb to the first node whose exit lies beyond the walk
+__device__ __forceinline__ void lpWalkAscend(const DevSlot& s, LpWalk& w) {
+    const float kVdel[3] = {1.f, 8.f, 128.f};
+    while (w.lev <= 2 && w.dda.t.x > (w.lev == 1 ? w.tMax1 : w.tMax2)) {
+        w.lev++;
+        if (w.lev <= 2) {
+            w.node = w.lev == 1 ? w.nid1 : 0;
+            w.vmin = nodeVmin(s, w.lev, w.node);
+            w.dda.prepare(w.vmin, kVdel[w.lev]);
+        }
+    }
+}
+// SampleDist::end
+__device__ __forceinline__ void lpWalkEnd(LpWalk& w, bool init) {
+    if (init) {
+        if (w.hit == -1) { w.hit = kRayTMax; w.tr = vr::exp_(-w.thick); w.pdf = w.tr; }
+    } else {
+        w.hit = kRayTMax; w.tr = 1.f; w.pdf = 1.f;
+    }
+}
+// trackVolume's set-up; false when the walk ended there (the ray misses the volume)
+__device__ __forceinline__ bool lpWalkStart(const DevSlot& s, int mip, const Ray& rWorld, LpWalk& w) {
+    Ray ray;
+    ray.o = mulPoint(rWorld.o, s.M);
+    ray.d = mulVec(rWorld.d, s.M);
+    ray.tMin = rWorld.tMin; ray.tMax = rWorld.tMax;
+    float tNear, tFar;
+    w.thick = 0.f;
+    if (!intersectBound(ray, tNear, tFar, mip, false)) { lpWalkEnd(w, false); return false; }
+    w.tFar = tFar;
+    w.hit = -1;
+    f3 tStart = mk3(tNear, tFar, 0);
+    w.vmin = mk3(0.f);
+    w.node = 0;
+    tStart.x += 0.01f;
+    w.tMax2 = tStart.y;
+    w.dda.setFromRay(ray.o, ray.d, tStart);
+    w.dda.prepare(w.vmin, 128.f);
+    w.t = tNear;
+    w.lev = 2;
+    w.oiter = 0;
+    w.inBrick = false;
+    return true;
+}
+// one step of the walk; true when it has ended (hit, tr and pdf hold the sample)
+__device__ __forceinline__ bool lpWalkStep(const DevSlot& s, int mip, LpWalk& w) {
+    const float eps = 0.01f;
+    if (w.inBrick) {
+        // one trip of SampleDist::mainStep's voxel loop (one sample, point-sampled)
+        if (!(w.biter < kMaxBrickSteps && inLeaf(w.dl.p))) {
+            w.inBrick = false;               // mainStep returned false: the node loop goes on
+            w.dda.step();
+            w.dda.t.x += eps;
+            lpWalkAscend(s, w);
+            w.oiter++;
+            return false;
+        }
+        w.dl.next();
+        const float maxDeltaT = vr::fmin_(w.tFar - w.t, w.dl.t.y - w.t);
+        const float curTMax = vr::fmin_(w.tFar, w.dl.t.y);
+        const float sigma_t = densityCell(mip, w.brick, w.dl.p) * c_scene.sigma_t;
+        const float dT = -vr::log_(1 - vr::next1D(w.g)) / sigma_t;
+        float curT = w.t + dT;
+        if (vr::isnan_(curT) || vr::isinf_(curT)) curT = kRayTMax;
+        if (curT < curTMax) {
+            w.hit = curT;
+            w.tr = vr::exp_(-(dT * sigma_t + w.thick));
+            w.pdf = sigma_t * w.tr;
+            return true;
+        }
+        const float dThick = maxDeltaT * sigma_t;
+        w.t = curTMax;
+        w.thick += dThick;
+        if (w.t >= w.tFar) { lpWalkEnd(w, true); return true; }
+        w.dl.step();
+        w.biter++;
+        return false;
+    }
+    // one trip of trackVolume's node loop
+    const int kDim[3] = {3, 4, 5}, kRes[3] = {8, 16, 32};
+    const float kVdel[3] = {1.f, 8.f, 128.f};
+    const int* p = w.dda.p;
+    if (!(w.oiter < 4096 && w.lev > 0 && w.lev <= 2 && p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && p[0] <= kRes[w.lev] && p[1] <= kRes[w.lev] &&
+          p[2] <= kRes[w.lev])) {
+        lpWalkEnd(w, true);
+        return true;
+    }
+    w.dda.next();
+    const int b = (((w.dda.p[2] << kDim[w.lev]) + w.dda.p[1]) << kDim[w.lev]) + w.dda.p[0];
+    const int child = getChild(s, w.node, w.lev, b);
+    if (child >= 0) {
+        if (w.lev == 1) {
+            w.t = w.dda.t.x - eps;
+            if (w.t >= w.tFar) { lpWalkEnd(w, true); return true; }
+            const f3 vl = nodeVmin(s, 0, child);
+            w.brick = child;
+            w.dl = w.dda;
+            w.dl.prepareLeaf(vl);
+            w.biter = 0;
+            w.inBrick = true;
+            return false;
+        }
+        w.lev--;
+        w.nid1 = child;
+        w.node = child;
+        w.vmin = nodeVmin(s, w.lev, child);
+        w.tMax1 = w.dda.t.y;
+        w.dda.prepare(w.vmin, kVdel[w.lev]);
+    } else {
+        w.dda.step();
+        w.dda.t.x += eps;
+    }
+    lpWalkAscend(s, w);
+    w.oiter++;
+    return false;
+}
+
+// the distance samples of the queue of bounce b (its sorted copy), written back into the entries
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+    const int n = min(L.pcount[b], L.pcapacity);
+    const SamplingOptions& o = P.initial;
+    int mip = o.visibilityMipLevel;
+    if (P.useCoarser) mip = min((o.visibilityMipLevel >= kNumMaxMips ? kNumMaxMips : 0) + c_scene.numMips - 1, mip + 1);
+    const DevSlot& s = c_scene.slots[mip];
+    const int lane = threadIdx.x & 31;
+    int* cursor = L.wcursor + b;
+    LpWalk w;
+    bool live = false, exhausted = false;
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !live && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(cursor, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!live && !exhausted) {
+                const int idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx >= n) exhausted = true;
+                else {
+                    w.entry = (size_t)idx;
+                    const float4* q = L.psort + 4 * w.entry;
+                    const float4 q0 = q[0], q1 = q[1], q3 = q[3];
+                    w.g.s[0] = __float_as_uint(q3.x); w.g.s[1] = __float_as_uint(q3.y);
+                    w.g.s[2] = __float_as_uint(q3.z); w.g.s[3] = __float_as_uint(q3.w);
+                    const Ray r{mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), 0.f, kRayTMax};
+                    live = true;
+                    if (!lpWalkStart(s, mip, r, w)) live = false, exhausted = false;
+                    if (!live) {
+                        float4* qw = L.psort + 4 * w.entry;
+                        qw[0].w *= w.pdf; qw[1].w *= w.tr; qw[2].z = w.hit;
+                        qw[3] = make_float4(__uint_as_float(w.g.s[0]), __uint_as_float(w.g.s[1]), __uint_as_float(w.g.s[2]), __uint_as_float(w.g.s[3]));
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, live) == 0) {
+            if (__ballot_sync(0xffffffffu, !exhausted) == 0) break;
+            continue;
+        }
+        if (live && lpWalkStep(s, mip, w)) {
+            float4* qw = L.psort + 4 * w.entry;
+            qw[0].w *= w.pdf; qw[1].w *= w.tr; qw[2].z = w.hit;
+            qw[3] = make_float4(__uint_as_float(w.g.s[0]), __uint_as_float(w.g.s[1]), __uint_as_float(w.g.s[2]), __uint_as_float(w.g.s[3]));
+            live = false;
+        }
+    }
+}
+
+// the vertices of the queue of bounce b from the distances k_lp_walk left in its entries
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+    const int n = min(L.pcount[b], L.pcapacity);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
+        const float4* q = L.psort + 4 * i;
+        const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
+        LpPath cs;
+        cs.ray = Ray{mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), 0.f, kRayTMax};
+        cs.pathPdf = q0.w; cs.pathPHat = q1.w; cs.primaryDepth = 0.f; cs.bounce = b;
+        const int pid = __float_as_int(q2.x), c = __float_as_int(q2.y);
+        vr::Rng g;
+        g.s[0] = __float_as_uint(q3.x); g.s[1] = __float_as_uint(q3.y); g.s[2] = __float_as_uint(q3.z); g.s[3] = __float_as_uint(q3.w);
+        // pdf and Tr are already in pathPdf and pathPHat: x * 1 = x
+        if (lpVertex<MB>(P, cs, q2.z, 1.f, 1.f, g, L, c, pid)) lpEnqueue(L, b + 1, cs, pid, c, g);
+    }
+}
+
 // Counting sort of a queue by coherence key before its bounce pass: the octant of the direction
 // and the 8^3 cell of the volume box holding the origin, so that a warp takes paths that cross
 // the same region in the same direction.  The order of a queue changes no result (every path
