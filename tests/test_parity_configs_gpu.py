@@ -1,0 +1,295 @@
+"""The GPU frame loop against the CPU oracle on the benchmark's own configurations, and the
+converged mean of the plain and learned forms against the FP64 path-traced reference.
+
+Configurations (each exactly as the benchmark defines it, through the C ABI):
+
+  cfg1  256x256, 128^3 dense fBm cloud, max path length 2, 8 candidates, temporal + 3 spatial
+        neighbours (radius 10), static camera, all 16 frames;
+  cfg2  1920x1080, 512^3 sparse fBm cloud in 8^3 bricks with its conservative pyramid, max path
+        length 3, 32 candidates, temporal + 3 spatial neighbours, 16 point lights + sky, the
+        orbiting camera, 2 frames (the second one runs temporal and spatial reuse on history);
+  cfg4  cfg1 with the learned target (2^20 training samples per frame, batch 16384), 4 frames,
+        bit-exact given the GPU's predicted transmittances, with the inference error bounded
+        and the selection flips it causes counted against the oracle's own CPU network;
+  cfg5  instances of the batched workload rendered by the batched persistent kernels (a fire
+        plume and a cloud, FP16 bricks, learned target) compared with the oracle directly.
+
+Bar: images, reservoirs (selection, M, weights, depths, light ids), extra-bounce suffixes and
+features bit-exact (the sampler's RNG stream is the reference's, so selected candidates, path
+indices and M counts agree exactly).
+
+Converged mean: 1024 frames of a form at a static camera, accumulated in FP64 (vr_accumulate),
+against a 65536-spp FP64 path tracer.  Per pixel the error of the mean is divided by its
+standard error (from the means of 16 blocks of 64 frames for ReSTIR, 16 blocks of 4096 spp for
+the path tracer); for an unbiased estimator those scores have unit variance.
+
+  * With an unbiased transmittance estimator in the final shading (ratio tracking, which walks
+    the cells the path tracer walks), the plain and the learned form are unbiased: mean squared
+    score <= 1.5, image-average radiance within 3 standard errors, relMSE of the mean at least
+    2.5x below that of a quarter of the frames; the learned mean also meets the first two bounds
+    against the plain mean (the learned target adds no bias).
+  * With the reference's default final shading (analytic transmittance of the trilinear field,
+    walking vertex-centred cells), the mean is brighter than the path tracer by about 0.25 % of
+    the image average: where an occupied brick borders an unallocated one, the two walks cover
+    different half-voxel shells of the field.  Bounds: relMSE of the mean <= 3e-4, image average
+    within 0.5 %.
+"""
+import numpy as np
+import pytest
+
+from tests.test_parity_gpu import FIELDS, _compare_frame, _same
+
+pytestmark = pytest.mark.gpu
+
+
+def _opts(vlib, sc, overrides=None):
+    from volumetricrestirrelease_gb300 import capi
+    o = capi.default_options(vlib)
+    for k, v in {**sc.options, **(overrides or {})}.items():
+        setattr(o, k, v)
+    return o
+
+
+def _pair(vlib, sc, vol, opts, temp=None):
+    from oracle.oracle import Oracle
+    from volumetricrestirrelease_gb300.restir import VolumetricReSTIR
+    gpu = VolumetricReSTIR(sc.width, sc.height, opts.as_dict(), lib=vlib)
+    gpu.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+    ora = Oracle(sc.width, sc.height, opts)
+    ora.set_volume(vol, sc.medium)
+    ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
+    if temp is not None:
+        gpu.setEmission(temp, *sc.fire[2:])
+        ora.set_emission(temp, *sc.fire[2:])
+    return gpu, ora
+
+
+def _compare_buffers(gpu, ora, opts, tag):
+    from volumetricrestirrelease_gb300.restir import as_reservoirs
+    for which in (0, 1) if opts.mEnableTemporalReuse else (0,):
+        rg = as_reservoirs(gpu.export_reservoirs(which), opts.mMaxBounces)
+        ro = ora.export_reservoirs(which)
+        for k in FIELDS:
+            assert _same(rg[k], ro[k]), f"{tag} buffer {which}: reservoir field {k} differs"
+        if opts.mMaxBounces > 1:
+            eg = gpu.export_extra(which).reshape(-1, opts.mMaxBounces - 1, 3)
+            eo = ora.export_extra(which).reshape(-1, opts.mMaxBounces - 1, 3)
+            nb = ro["sampledPixel"] >> 20
+            for b in range(opts.mMaxBounces - 1):
+                m = nb > b
+                assert _same(eg[m, b], eo[m, b]), f"{tag} buffer {which}: extra bounce {b} differs"
+
+
+def test_cfg1_all_16_frames_bit_exact(vlib, cuda):
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume
+    sc = scenes.small()                       # 256x256, M = 8, path length 2, k = 4, r = 10
+    assert (sc.width, sc.height, sc.frames) == (256, 256, 16) and sc.orbit_deg_per_frame == 0.0
+    vol = Volume.procedural(sc.volume, lib=vlib)
+    opts = _opts(vlib, sc)
+    assert (opts.mInitialM, opts.mMaxBounces, opts.mSpatialSampleCount, opts.mSampleRadius) == (8, 2, 4, 10.0)
+    gpu, ora = _pair(vlib, sc, vol, opts)
+    for f in range(sc.frames):
+        img = _compare_frame(gpu, ora, opts, cuda, sc.camera(f), f)
+    assert img[..., :3].mean() > 0.05
+
+
+def test_cfg2_1080p_two_frames_bit_exact(vlib, cuda):
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume
+    sc = scenes.full()                        # 1920x1080, 512^3 sparse, M = 32, path length 3
+    vol = Volume.procedural(sc.volume, lib=vlib)
+    opts = _opts(vlib, sc)
+    assert (sc.width, sc.height, opts.mInitialM, opts.mMaxBounces) == (1920, 1080, 32, 3)
+    gpu, ora = _pair(vlib, sc, vol, opts)
+    for f in range(2):
+        img = _compare_frame(gpu, ora, opts, cuda, sc.camera(f), f)
+    assert img[..., :3].mean() > 0.05
+
+
+def test_cfg4_learned_256_four_frames(vlib, cuda):
+    from oracle.oracle import Oracle, net_forward
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume, as_reservoirs
+    sc = scenes.small()
+    vol = Volume.procedural(sc.volume, lib=vlib)
+    opts = _opts(vlib, sc, dict(mUseLearnedPHat=1))
+    assert (opts.mLearnedTrainSamples, opts.mLearnedBatch) == (1 << 20, 16384)
+    gpu, ora = _pair(vlib, sc, vol, opts)
+    out = cuda.empty((sc.height, sc.width, 4), device="cuda", dtype=cuda.float32)
+    for f in range(4):
+        cam = sc.camera(f)
+        params, box = gpu.net_params(), gpu.net_box()         # the weights this frame infers with
+        gpu.execute(cam, out.data_ptr())
+        cuda.cuda.synchronize()
+        img = out.cpu().numpy()
+        T, qg, tg = gpu.export_learned(0), gpu.export_learned(1), gpu.export_learned(2)
+        slots = qg[:, 7].view(np.int32)
+        # tensor-core inference against the CPU network with the same weights (the tensor
+        # cores sum the BF16 products in another order): 99.9 % of the queries within 1e-2
+        # relative, every query within 5e-2
+        tcpu = net_forward(params, box, opts.mLearnedTFloor, qg)
+        rel = np.abs(T[slots] - tcpu) / tcpu
+        q = np.quantile(rel, [0.5, 0.999, 1.0])
+        print(f"frame {f}: {len(slots)} queries, relative error of T: median {q[0]:.2e}, 99.9 % {q[1]:.2e}, max {q[2]:.2e}")
+        assert q[1] < 1e-2 and q[2] < 5e-2, q
+        if f == 0:
+            # selection flips caused by that error: the oracle with its own CPU network on the
+            # same first frame (no history yet) against the GPU's reservoirs
+            own = Oracle(sc.width, sc.height, opts)
+            own.set_volume(vol, sc.medium)
+            own.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
+            own.set_net(params, box)
+            own.render_frame(cam)
+            rg = as_reservoirs(gpu.export_reservoirs(0), opts.mMaxBounces)
+            ro = own.export_reservoirs(0)
+            flips = int(((rg["sampledPixel"] != ro["sampledPixel"]) | (rg["lightID"] != ro["lightID"])
+                         | (rg["depth"].view(np.uint32) != ro["depth"].view(np.uint32))).sum())
+            print(f"frame 0: {flips} of {sc.width * sc.height} pixels select a different sample with the CPU network's T")
+            assert flips <= 0.01 * sc.width * sc.height, f"{flips} of {sc.width * sc.height} pixels select differently"
+        ora.set_lp_T(T)
+        ref = ora.render_frame(cam)
+        nbad = int((img.view(np.uint32) != ref.view(np.uint32)).any(-1).sum())
+        assert nbad == 0, f"frame {f}: {nbad} pixels differ from the oracle given the GPU's T"
+        assert _same(tg, ora.export_lp(2)), f"frame {f}: training samples differ"
+        _compare_buffers(gpu, ora, opts, f"frame {f}")
+        assert not _same(params, gpu.net_params()), "the frame's training steps did not change the weights"
+    assert img[..., :3].mean() > 0.05
+
+
+def test_cfg5_batch_instances_against_oracle(vlib, cuda):
+    """A fire plume (512x512, 128^3, 27 candidates) and a cloud (256x256, 448^3, 19 candidates)
+    of the batched workload, with a second plume, rendered by the batched kernels from the
+    captured graph; each instance's frames against the oracle given that instance's T."""
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Batch, VolumetricReSTIR, as_reservoirs
+    descs = scenes.batch()
+    picked = [0, 2, 8]
+    assert descs[0].fire and descs[2].fire and not descs[8].fire
+    insts = []
+    for i in picked:
+        sc = descs[i]
+        vol, temp = scenes.make_volumes(sc, vlib)
+        opts = _opts(vlib, sc)
+        r = VolumetricReSTIR(sc.width, sc.height, opts.as_dict(), lib=vlib)
+        r.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        if temp is not None:
+            r.setEmission(temp, *sc.fire[2:])
+        from oracle.oracle import Oracle
+        ora = Oracle(sc.width, sc.height, opts)
+        ora.set_volume(vol, sc.medium)
+        ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
+        if temp is not None:
+            ora.set_emission(temp, *sc.fire[2:])
+        insts.append((sc, (vol, temp), opts, r, ora))
+    batch = Batch([x[3] for x in insts], graph=True)
+    outs = [cuda.empty((x[0].height, x[0].width, 4), device="cuda", dtype=cuda.float32) for x in insts]
+    for f in range(3):
+        batch.render([x[0].camera(f) for x in insts], [o.data_ptr() for o in outs])
+        cuda.cuda.synchronize()
+        for k, (sc, vols, opts, r, ora) in enumerate(insts):
+            if picked[k] == 2:
+                continue                      # rendered alongside; two instances are checked
+            ora.set_lp_T(r.export_learned(0))
+            ref = ora.render_frame(sc.camera(f))
+            img = outs[k].cpu().numpy()
+            nbad = int((img.view(np.uint32) != ref.view(np.uint32)).any(-1).sum())
+            assert nbad == 0, f"instance {picked[k]}, frame {f}: {nbad} pixels differ from the oracle"
+            rg = as_reservoirs(r.export_reservoirs(0), opts.mMaxBounces)
+            ro = ora.export_reservoirs(0)
+            for key in FIELDS:
+                assert _same(rg[key], ro[key]), f"instance {picked[k]}, frame {f}: reservoir field {key} differs"
+    assert outs[0].cpu().numpy()[..., :3].max() > 0
+
+
+# ---------------------------------------------------------------------------------------------
+# converged mean
+# ---------------------------------------------------------------------------------------------
+CW = CH = 64
+BLOCKS = 16
+FRAMES = 1024
+REF_SPP_BLOCK = 4096
+
+
+def _block_means(vlib, cuda, ctx, cam, frames, blocks):
+    """Per-block means (blocks, H, W, 3) of `frames` consecutive frames, each block accumulated
+    in FP64 by vr_accumulate."""
+    from volumetricrestirrelease_gb300.restir import Accumulator
+    per = frames // blocks
+    out = cuda.empty((CH, CW, 4), device="cuda", dtype=cuda.float32)
+    mean = cuda.empty((CH, CW, 4), device="cuda", dtype=cuda.float32)
+    acc = Accumulator(CW, CH, precision=0, lib=vlib)
+    means = []
+    for b in range(blocks):
+        acc.reset()
+        for i in range(per):
+            ctx.execute(cam, out.data_ptr())
+            acc.add(out.data_ptr(), mean.data_ptr() if i == per - 1 else None)
+        assert acc.count == per
+        cuda.cuda.synchronize()
+        means.append(mean.cpu().numpy()[..., :3].astype(np.float64))
+    return np.stack(means)
+
+
+def _scores(a_blocks, b_blocks):
+    """Per-pixel error of mean(a) - mean(b) over its standard error (mean of the squares), the
+    image-average difference over its standard error, and the image-average relative difference.
+    Pixels where both estimates are constant (the background, seen unattenuated) are scored
+    against a floor of 1e-6 of the value."""
+    ma, mb = a_blocks.mean(0), b_blocks.mean(0)
+    va = a_blocks.var(0, ddof=1) / len(a_blocks)
+    vb = b_blocks.var(0, ddof=1) / len(b_blocks)
+    se = np.sqrt(va + vb) + 1e-6 * np.abs(mb) + 1e-12
+    z = (ma - mb) / se
+    ga, gb = a_blocks.mean(axis=(1, 2, 3)), b_blocks.mean(axis=(1, 2, 3))
+    gz = (ga.mean() - gb.mean()) / np.sqrt(ga.var(ddof=1) / len(ga) + gb.var(ddof=1) / len(gb))
+    return float(np.mean(z ** 2)), float(gz), float((ga.mean() - gb.mean()) / gb.mean())
+
+
+def _relmse(x, ref):
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def test_converged_mean_matches_fp64_reference(vlib, cuda):
+    from volumetricrestirrelease_gb300 import scenes
+    from volumetricrestirrelease_gb300.restir import Volume, VolumetricReSTIR
+    sc = scenes.small(width=CW, height=CH)
+    vol = Volume.procedural(sc.volume, lib=vlib)
+    cam = sc.camera(0)
+
+    def ctx(over=None):
+        r = VolumetricReSTIR(CW, CH, _opts(vlib, sc, over).as_dict(), lib=vlib)
+        r.setScene(vol, sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
+        return r
+    # FP64 path tracer: 16 blocks of 4096 samples per pixel
+    rd = ctx()
+    ref_blocks = []
+    for b in range(BLOCKS):
+        acc = cuda.zeros((CH, CW, 3), device="cuda", dtype=cuda.float64)
+        for f0 in range(0, REF_SPP_BLOCK, 512):
+            rd.render_reference(cam, acc.data_ptr(), b * REF_SPP_BLOCK + f0, 512)
+        cuda.cuda.synchronize()
+        ref_blocks.append(acc.cpu().numpy() / REF_SPP_BLOCK)
+    ref_blocks = np.stack(ref_blocks)
+    ref = ref_blocks.mean(0)
+    ratio = dict(mFinalVisibilityTrackingMethod=0, mFinalLightTrackingMethod=0)
+    learned = dict(mUseLearnedPHat=1, mLearnedTrainSamples=65536, mLearnedBatch=16384)
+    forms = {"plain, final ratio tracking": ratio, "learned, final ratio tracking": {**ratio, **learned},
+             "plain, default final shading": {}}
+    res = {}
+    for name, over in forms.items():
+        blocks = _block_means(vlib, cuda, ctx(over), cam, FRAMES, BLOCKS)
+        z2, gz, rel = _scores(blocks, ref_blocks)
+        full, quarter = _relmse(blocks.mean(0), ref), _relmse(blocks[:BLOCKS // 4].mean(0), ref)
+        res[name] = blocks
+        print(f"{name}: mean z^2 {z2:.3f}, image average {100 * rel:+.3f} % (z {gz:+.2f}), relMSE of the mean "
+              f"{full:.2e} ({FRAMES} frames) / {quarter:.2e} ({FRAMES // 4} frames)")
+        if "ratio" in name:
+            assert z2 <= 1.5, f"{name}: per-pixel errors of the mean exceed their standard errors (mean z^2 {z2:.3f})"
+            assert abs(gz) <= 3.0, f"{name}: image-average radiance off by {gz:.2f} standard errors"
+            assert full * 2.5 <= quarter, f"{name}: relMSE of the mean stops falling ({quarter:.2e} -> {full:.2e})"
+        else:
+            assert full <= 3e-4 and abs(rel) <= 5e-3, (full, rel)
+    z2, gz, rel = _scores(res["learned, final ratio tracking"], res["plain, final ratio tracking"])
+    print(f"learned vs plain: mean z^2 {z2:.3f}, image average {100 * rel:+.3f} % (z {gz:+.2f})")
+    assert z2 <= 1.5 and abs(gz) <= 3.0, (z2, gz)

@@ -417,6 +417,38 @@ class Batch:
             self._h = None
 
 
+class Accumulator:
+    """Running per-pixel sums of RGBA32F frames (AccumulatePass, Accumulate.cs.slang:55-125):
+    precision 0 = double, 1 = single, 2 = compensated single."""
+
+    def __init__(self, width, height, precision=0, lib=None):
+        self._lib = lib or capi.load()
+        h = C.c_void_p()
+        rc = self._lib.vr_accumulator_create(width, height, precision, C.byref(h))
+        if rc != capi.VR_OK:
+            raise RuntimeError(f"vr_accumulator_create failed ({rc})")
+        self._h = h
+
+    def add(self, frame_ptr, mean_out_ptr=None, stream=0):
+        """Adds one device frame; writes the running mean to mean_out_ptr (device RGBA32F) if given."""
+        rc = self._lib.vr_accumulate(self._h, C.c_void_p(frame_ptr), C.c_void_p(mean_out_ptr) if mean_out_ptr else None,
+                                     C.c_void_p(stream))
+        if rc != capi.VR_OK:
+            raise RuntimeError(f"vr_accumulate failed ({rc})")
+
+    def reset(self):
+        self._lib.vr_accumulator_reset(self._h)
+
+    @property
+    def count(self):
+        return self._lib.vr_accumulator_count(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.vr_accumulator_destroy(self._h)
+            self._h = None
+
+
 RESERVOIR_DTYPE_36 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
                                ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4"),
                                ("extraBounceStartId", "<i4")])
