@@ -6,21 +6,28 @@ lights + procedural sky, camera orbiting 0.5 deg per frame.  Synthetic data (the
 clouds are not available).
 
 Metric: 1080p frames/s of the learned-target form (transmittance MLP in the initial RIS target,
-FP16 bricks) at a relMSE against the FP64 path-traced reference matched to the plain form's
-(FP32 bricks, 32 candidates).  The match is made in the run: the relMSE of each form is measured
-at 480x270 on a static camera over frames 16..127 against a 1024-spp FP64 reference rendered on
-the GPU, and the learned form takes the smallest candidate count in {24, 28, 32, 36, 40, 48} whose relMSE
-is not above the plain form's by more than two standard errors of the difference (block means
-of 16 frames).  The plain form's frames/s is reported beside it.
+FP16 bricks) with LEARNED_M candidates, the count at which its relMSE against the FP64
+path-traced reference matches the plain form's (FP32 bricks, 32 candidates).  The match is
+checked in the run: both forms render the orbiting camera path at 960x540 for 128 frames, and
+at every 8th frame from 32 on each image's relMSE is taken against a 512-spp FP64 reference of
+that frame rendered on the GPU.  The learned form at candidate count M matches when the mean of
+the per-frame differences (learned - plain) is at most one standard error of that mean above
+zero; the sweep over several M also gives the count at equal relMSE by interpolation.  The plain
+form's frames/s is reported beside the learned form's.
 
 Output: one JSON line (rank 0).  `value` = frames/s with every input resident in HBM
 (vr_render_frame into a device buffer, CUDA events on the launching stream); `e2e` = the same
 frames through vr_render_frame_host_async, every image copied back to pinned host memory
-inside the timed region (the copy of a frame overlaps the next frame's kernels).  The working set (bricks of all mip slots + reservoir/history buffers) is
-larger than the 129 MB L2, so no explicit flush is done between frames.
+inside the timed region (the copy of a frame overlaps the next frame's kernels).  The working
+set (bricks of all mip slots + reservoir/history buffers) is larger than the 129 MB L2, so no
+explicit flush is done between frames.
 
 `--impl reference` times the CPU restatement of the reference shader logic (the reference
-itself is D3D12/Slang-only) on all host cores over a bounded sample of the same workload.
+itself is D3D12/Slang-only) on all host cores: full 1920x1080 frames of the same learned form
+(LEARNED_M candidates, FP16 bricks, the network trained on the host by the same 64 Adam steps
+per frame), with its input grid built by the oracle's own library; the plain form is timed
+beside it.  It renders as many of the requested frames as fit a time budget and reports the
+frames it timed.
 
 Multi-GPU: the frame loop does not shard across GPUs here; N ranks run N independent
 replicas (weak scaling, no collective) and `value` sums their frames.
@@ -44,7 +51,10 @@ METRIC = "1080p frames/s at matched relMSE vs FP64 ref; learned-p-hat vs plain, 
 WORKLOAD = ("learned-p-hat + FP16-brick ReSTIR frame, 1920x1080, 512^3 sparse fBm (8^3 bricks, 4-level conservative mips), "
             "max path length 3, temporal + 3 spatial neighbours, 16 point lights + 512x256 sky, orbiting camera; "
             "candidate count matched to the plain form's relMSE (plain: FP32 bricks, M=32)")
-LEARNED_M = (24, 28, 32, 36, 40, 48)
+# the learned form's candidate count: the quality sweep (960x540, orbiting camera) finds its
+# relMSE not above the plain form's (32 candidates) by more than one standard error at this count
+LEARNED_M = 36
+SWEEP_M = (28, 32, 36, 40, 48)
 
 
 def _peaks():
@@ -171,58 +181,88 @@ def generate_stream_bytes_per_pixel(M, vertices_px, queries_px):
 
 
 NET_FLOP_PER_QUERY = 4 * 2 * 64 * 64 + 2 * 64      # four 64x64 layers and the output dot product
+# the plain path's reservoir and feature stream per pixel and frame (path length 3, 4 spatial
+# taps): the SoA bytes its two fused kernels read and write, by stream_bytes_per_pixel
+SURVEY_STREAM_PX = sum(stream_bytes_per_pixel(3, 4).values())
 
 
 def _relmse(img, ref):
     return float(np.mean((img[..., :3].astype(np.float64) - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-def quality(lib, vols, args, forms, QW=480, QH=270, frames=128, first=16, spp=1024, block=16):
-    """relMSE of each form against an FP64 path-traced reference at QWxQH, static camera,
-    averaged over frames first..frames-1, with the standard error of that mean from the means of
-    blocks of `block` consecutive frames (consecutive frames are correlated through temporal
-    reuse).  forms: {name: (fp16, learned, M[, volume key])} -> {name: (mean, standard error)}."""
+def quality(lib, vols, args, forms, QW=960, QH=540, frames=128, first=32, every=8, spp=512):
+    """relMSE of each form against an FP64 path-traced reference at QWxQH on the orbiting camera
+    path of the timed workload: every form renders frames 0..frames-1, and at frames first,
+    first+every, ... each image is compared with a `spp`-sample FP64 reference of that frame.
+    forms: {name: (fp16, learned, M[, volume key])} -> ({name: per-frame relMSE array}, info)."""
     import torch
     from volumetricrestirrelease_gb300.restir import VolumetricReSTIR
-    sc = _scene(args, static=True, width=QW, height=QH)
+    sc = _scene(args, width=QW, height=QH)
+    evals = list(range(first, frames, every))
     rd = VolumetricReSTIR(QW, QH, _options(lib, sc).as_dict(), lib=lib)
     rd.setScene(vols[False], sc.medium, sc.lights, sc.env_rgb, sc.env_scale)
-    acc = torch.zeros((QH, QW, 3), device="cuda", dtype=torch.float64)
-    for f0 in range(0, spp, 64):
-        rd.render_reference(sc.camera(0), acc.data_ptr(), f0, min(64, spp - f0))
-    torch.cuda.synchronize()
-    ref = (acc / spp).cpu().numpy()
+    refs = {}
+    for f in evals:
+        acc = torch.zeros((QH, QW, 3), device="cuda", dtype=torch.float64)
+        for f0 in range(0, spp, 128):
+            rd.render_reference(sc.camera(f), acc.data_ptr(), f0, min(128, spp - f0))
+        torch.cuda.synchronize()
+        refs[f] = (acc / spp).cpu().numpy()
     del rd
     out = torch.empty((QH, QW, 4), device="cuda")
-    res = {}
-    plain_imgs = {}
-    vs_fp32 = {}
+    res, plain_imgs, vs_fp32 = {}, {}, {}
     for name, form in forms.items():
         fp16, learned, M = form[:3]
         vkey = form[3] if len(form) > 3 else fp16
-        scf = _scene(args, fp16=fp16, static=True, width=QW, height=QH)
+        scf = _scene(args, fp16=fp16, width=QW, height=QH)
         rd = VolumetricReSTIR(QW, QH, _options(lib, scf, learned, M).as_dict(), lib=lib)
         rd.setScene(vols[vkey], scf.medium, scf.lights, scf.env_rgb, scf.env_scale)
         errs, cross = [], []
         for f in range(frames):
             rd.execute(scf.camera(f), out.data_ptr())
-            if f >= first:
+            if f in refs:
                 torch.cuda.synchronize()
                 img = out.cpu().numpy()
-                errs.append(_relmse(img, ref))
+                errs.append(_relmse(img, refs[f]))
                 if name == "plain":
                     plain_imgs[f] = img[..., :3].astype(np.float64)
                 elif name in ("plain_fp16", "plain_bc4") and f in plain_imgs:
                     cross.append(_relmse(img, plain_imgs[f]))
         if cross:
             vs_fp32[name] = float(np.mean(cross))
-        e = np.asarray(errs)
-        bm = e[: len(e) // block * block].reshape(-1, block).mean(1)
-        res[name] = (float(e.mean()), float(bm.std(ddof=1) / np.sqrt(len(bm))))
+        res[name] = np.asarray(errs)
         del rd
-    return res, {"fp16_vs_fp32_relmse": vs_fp32.get("plain_fp16"), "bc4_vs_fp32_relmse": vs_fp32.get("plain_bc4"), "resolution": f"{QW}x{QH}", "camera": "static (frame 0 of the orbit)", "frames": f"{first}..{frames - 1}",
-                 "reference": f"{spp} spp FP64 path tracer on the GPU", "relmse": "mean over pixels and RGB of (x-r)^2/(r^2+0.01)",
-                 "standard_error": f"from the means of blocks of {block} frames"}
+    info = {"fp16_vs_fp32_relmse": vs_fp32.get("plain_fp16"), "bc4_vs_fp32_relmse": vs_fp32.get("plain_bc4"),
+            "resolution": f"{QW}x{QH}", "camera": "orbiting 0.5 deg per frame (the timed path)",
+            "frames": f"{len(evals)} frames ({first}, {first + every}, ..., {evals[-1]}) of {frames}",
+            "reference": f"{spp} spp FP64 path tracer on the GPU, per evaluated frame",
+            "relmse": "mean over pixels and RGB of (x-r)^2/(r^2+0.01)",
+            "standard_error": "of the mean over the evaluated frames of the per-frame difference to the plain form"}
+    return res, info
+
+
+def match_candidates(rel, sweep):
+    """The paired comparison of each learned count with the plain form: mean per-frame relMSE
+    difference, its standard error, z = mean / SE, and the count at equal relMSE interpolated
+    linearly in 1/M between the sweep's neighbours."""
+    p = rel["plain"]
+    out = {}
+    for M in sweep:
+        d = rel[f"learned_M{M}"] - p
+        se = float(d.std(ddof=1) / np.sqrt(len(d))) if len(d) > 1 else float("inf")
+        out[M] = {"relmse": float(rel[f"learned_M{M}"].mean()), "diff": float(d.mean()), "se": se,
+                  "z": float(d.mean() / se) if se > 0 else float("inf")}
+    equal = None
+    ms = sorted(sweep)
+    for a, b in zip(ms, ms[1:]):
+        da, db = out[a]["diff"], out[b]["diff"]
+        if da > 0 >= db:
+            t = da / (da - db)
+            equal = 1.0 / (1.0 / a + t * (1.0 / b - 1.0 / a))
+            break
+    if equal is None and out[ms[0]]["diff"] <= 0:
+        equal = float(ms[0])
+    return out, equal
 
 
 def _time_frames(rd, sc, out, sptr, warmup, steps, first=0, clock_index=None, barrier=lambda: None):
@@ -255,90 +295,111 @@ def _time_frames(rd, sc, out, sptr, warmup, steps, first=0, clock_index=None, ba
     return ms, [t / max(nfr, 1) for t in tot], launches, (clk.summary() if clk else None)
 
 
-def cpu_sample(args, threads, frames=2, scale_w=4, scale_h=4, learned=None):
-    """Times the oracle (CPU restatement) on a reduced-resolution run of the plain form of the
-    same scene: frame 0 untimed, frame 1 timed (temporal + spatial), scaled by pixel count.
-    With learned = (M, params, box) it also runs the learned form (CPU network) for the
-    per-pixel voxel reads, vertex records and queries of the generate kernel."""
+def _oracle_frames(args, threads, learned, M, warm, timed, budget_s=None):
+    """Full-resolution frames of the workload on the oracle (the CPU restatement) on `threads`
+    host cores, with the input grid built by the oracle's own library.  learned: the learned
+    form (FP16 bricks), the network trained on the host after every frame by the frame's 64
+    Adam steps, as the GPU form does.  Returns the wall-clock seconds of each timed frame
+    (render + training), after `warm` untimed frames; with budget_s, stops once the timed frames
+    have used it (at least two timed frames)."""
     from oracle import oracle as O
-    from volumetricrestirrelease_gb300 import capi
-    from volumetricrestirrelease_gb300.restir import Volume
-    lib = capi.load()
-    W, H = args.width // scale_w, args.height // scale_h
-    sc = _scene(args, width=W, height=H)
-    vol = Volume.procedural(sc.volume, lib=lib)
-    ora = O.Oracle(W, H, _options(lib, sc), threads=threads)
+    sc = _scene(args, fp16=learned)
+    vol = O.OracleVolume(sc.volume)
+    over = dict(sc.options, mInitialM=M)
+    if learned:
+        over["mUseLearnedPHat"] = 1
+    opts = O.default_options(**over)
+    ora = O.Oracle(args.width, args.height, opts, threads=threads)
     ora.set_volume(vol, sc.medium)
     ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
-    ora.render_frame(sc.camera(0))
-    O.voxel_reads()
-    times = []
-    for f in range(1, frames):
-        t = time.perf_counter()
+    trainer, box = None, None
+    if learned:
+        info = vol.info()
+        box = (np.asarray(info.world_min, np.float32), np.full(3, 1.0 / (info.res * info.voxel_size), np.float32))
+        trainer = O.CpuTrainer(O.net_init(opts.mLearnedSeed), box, lr=opts.mLearnedLearningRate, threads=threads)
+    steps = opts.mLearnedTrainSamples // opts.mLearnedBatch
+
+    def frame(f):
+        if learned:
+            ora.set_net(trainer.w, box)
         ora.render_frame(sc.camera(f))
+        if learned:
+            smp = ora.export_lp(2)
+            for k in range(steps):
+                trainer.step(smp[k * opts.mLearnedBatch:(k + 1) * opts.mLearnedBatch])
+    for f in range(warm):
+        frame(f)
+    times = []
+    t_all = time.perf_counter()
+    for f in range(warm, warm + timed):
+        t = time.perf_counter()
+        frame(f)
         times.append(time.perf_counter() - t)
-    reads = O.voxel_reads()
-    t = float(np.median(times))
-    fps = 1.0 / (t * (args.width * args.height) / (W * H))
-    per_px = reads.astype(np.float64) / (W * H * len(times))
-    lp = None
-    if learned is not None:
-        M, params, box = learned
-        scl = _scene(args, fp16=True, width=W, height=H)
-        voll = Volume.procedural(scl.volume, lib=lib)
-        ol = O.Oracle(W, H, _options(lib, scl, True, M), threads=threads)
-        ol.set_volume(voll, scl.medium)
-        ol.set_lights(scl.lights, scl.env_rgb, scl.env_scale)
-        ol.set_net(params, box)
-        ol.render_frame(scl.camera(0))
-        O.voxel_reads()
-        ol.render_frame(scl.camera(1))
-        r = O.voxel_reads().astype(np.float64) / (W * H)
-        q = ol.export_lp(0)
-        lp = {"generate_voxel_reads_px": float(r[0] + r[1]), "select_voxel_reads_px": float(r[7] + r[2]),
-              "vertices_px": float(ol.export_lp(3)[0]) / (W * H), "queries_px": float((q[:, 6] >= 0).sum()) / (W * H)}
-    return fps, t, W, H, per_px, lp
+        if budget_s is not None and len(times) >= 2 and time.perf_counter() - t_all > budget_s:
+            break
+    return times
+
+
+def roofline_counts(args, threads, M, params, box, scale=4):
+    """Per-pixel voxel reads, vertex records and queries of the learned form's generate stage,
+    counted by the oracle on frame 1 at a quarter of the resolution per axis."""
+    from oracle import oracle as O
+    W, H = args.width // scale, args.height // scale
+    sc = _scene(args, fp16=True, width=W, height=H)
+    vol = O.OracleVolume(sc.volume)
+    ol = O.Oracle(W, H, O.default_options(**dict(sc.options, mUseLearnedPHat=1, mInitialM=M)), threads=threads)
+    ol.set_volume(vol, sc.medium)
+    ol.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
+    ol.set_net(params, box)
+    ol.render_frame(sc.camera(0))
+    O.voxel_reads()
+    ol.render_frame(sc.camera(1))
+    r = O.voxel_reads().astype(np.float64) / (W * H)
+    q = ol.export_lp(0)
+    return {"generate_voxel_reads_px": float(r[0] + r[1]), "select_voxel_reads_px": float(r[7] + r[2]),
+            "vertices_px": float(ol.export_lp(3)[0]) / (W * H), "queries_px": float((q[:, 6] >= 0).sum()) / (W * H),
+            "counted_at": f"{W}x{H}"}
 
 
 def run_reference(args):
-    """CPU restatement of the reference shaders on all host cores.  Each step renders one frame
-    of the workload at a quarter of the resolution per axis (after the previous frames built the
-    temporal history), and frames/s is scaled by the pixel count."""
+    """The CPU restatement of the reference shaders on all host cores, on the workload itself:
+    full 1920x1080 frames of the learned form at LEARNED_M candidates (FP16 bricks, host-side
+    training), as many of the requested frames as fit the time budget; then the plain form (FP32
+    bricks, 32 candidates) on two frames beside it.  Uses the oracle's library only."""
     ws, rank = _dist()
     if rank != 0:
         return
-    from oracle import oracle as O
-    from volumetricrestirrelease_gb300 import build as vbuild
-    from volumetricrestirrelease_gb300 import capi
-    from volumetricrestirrelease_gb300.restir import Volume
-    vbuild.build()
-    lib = capi.load()
+    from oracle import build as obuild
+    obuild.build()
     threads = os.cpu_count() or 1
-    W, H = args.width // 4, args.height // 4
-    sc = _scene(args, width=W, height=H)
-    vol = Volume.procedural(sc.volume, lib=lib)
-    ora = O.Oracle(W, H, _options(lib, sc), threads=threads)
-    ora.set_volume(vol, sc.medium)
-    ora.set_lights(sc.lights, sc.env_rgb, sc.env_scale)
-    for f in range(max(args.warmup, 1)):
-        ora.render_frame(sc.camera(f))
-    times = []
-    for f in range(max(args.warmup, 1), max(args.warmup, 1) + args.steps):
-        t = time.perf_counter()
-        ora.render_frame(sc.camera(f))
-        times.append(time.perf_counter() - t)
-    scale = (args.width * args.height) / (W * H)
-    fps = args.steps / (sum(times) * scale)
-    sample = (f"oracle (CPU restatement of the reference shaders; the reference itself is D3D12/Slang-only), plain form "
-              f"(FP32 bricks, M=32), {args.steps} frames at {W}x{H} after {max(args.warmup, 1)} untimed, scaled by pixel count "
-              f"to {args.width}x{args.height}")
-    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / fps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": args.width, "height": args.height},
-            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port", "sample": sample},
-            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    warm = min(max(args.warmup, 0), 1)
+    t0 = time.perf_counter()
+    times = _oracle_frames(args, threads, True, LEARNED_M, warm, args.steps, budget_s=args.ref_budget_s)
+    fps = len(times) / sum(times)
+    ptimes = _oracle_frames(args, threads, False, 32, 1, 2)
+    pfps = len(ptimes) / sum(ptimes)
+    sample = (f"oracle (CPU restatement of the reference shaders; the reference itself is D3D12/Slang-only) on {threads} "
+              f"host threads: {len(times)} full {args.width}x{args.height} frames of the learned form (M={LEARNED_M}, FP16 "
+              f"bricks, 64 host Adam steps per frame) after {warm} untimed, of {args.steps} requested within a "
+              f"{args.ref_budget_s:.0f} s budget")
+    line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": ws, "steps": len(times),
+            "warmup": warm, "ms_per_step": 1000.0 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (bf16 MLP, fp16 bricks)", "data": "synthetic",
+            "plain": {"value": pfps, "unit": "frames/s", "frames": len(ptimes), "candidates": 32, "bricks": "fp32",
+                      "ms_per_frame": [1000.0 * t for t in ptimes]},
+            "config": _config(args, LEARNED_M, ws),
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port", "sample": sample,
+                             "ms_per_frame": [1000.0 * t for t in times], "requested_steps": args.steps},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
     print(json.dumps(line), flush=True)
+
+
+def _config(args, M, ws=1):
+    """The workload's config, the same dict in both arms."""
+    return {"workload": WORKLOAD, "width": args.width, "height": args.height, "max_path_length": 3, "candidates": M,
+            "spatial_samples": 4, "bricks": "fp16", "l2": "inputs larger than L2 (bricks + reservoir buffers), no flush",
+            "parallelism": f"replicas x{ws}"}
 
 
 def _traffic_from_profile(kernel):
@@ -456,9 +517,10 @@ def run_small_configs(args, lib):
                 imgs32[f] = img[..., :3].astype(np.float64)
             elif name in ("cfg3_plain_fp16", "cfg3_plain_bc4"):
                 cross.append(_relmse(img, imgs32[f]))
-        res[name] = {"frames_per_s": 1000.0 / ms, "relmse_per_frame": errs, "relmse_frames_8_15": float(np.mean(errs[8:]))}
+        res[name] = {"frames_per_s": 1000.0 / ms, "relmse_frames_8_15": float(np.mean(errs[8:])),
+                     "relmse_range": [float(np.min(errs)), float(np.max(errs))]}
         if cross:
-            res[name]["relmse_vs_fp32_per_frame"] = cross
+            res[name]["relmse_vs_fp32_range"] = [float(np.min(cross)), float(np.max(cross))]
         del r, r2
     # the oracle on the host cores, cfg1, all 16 frames
     threads = os.cpu_count() or 1
@@ -564,26 +626,14 @@ def run_gpu(args):
         if ws > 1:
             torch.distributed.barrier()
 
-    # ---- relMSE matching (480x270, static camera, FP64 reference) ----
+    # ---- relMSE matching (960x540, the orbiting camera path, per-frame FP64 references) ----
     forms = {"plain": (False, False, 32), "plain_fp16": (True, False, 32), "plain_bc4": (False, False, 32, "bc4")}
-    for M in LEARNED_M:
+    for M in SWEEP_M:
         forms[f"learned_M{M}"] = (True, True, M)
     rel, qinfo = quality(lib, vols, args, forms) if not args.no_quality else ({}, {})
-    # matched: the learned form's relMSE is not above the plain form's by more than two standard
-    # errors of the difference
-    M_sel, matched = 32, False              # without the quality sweep: the plain form's count
-    if rel:
-        pm, pse = rel["plain"]
-
-        def z(M):
-            lm, lse = rel[f"learned_M{M}"]
-            return (lm - pm) / max(np.hypot(lse, pse), 1e-12)
-        ok = [M for M in LEARNED_M if z(M) <= 2.0]
-        if ok:
-            M_sel, matched = ok[0], True
-        else:
-            M_sel = min(LEARNED_M, key=z)
-
+    match, m_equal = match_candidates(rel, SWEEP_M) if rel else ({}, None)
+    M_sel = LEARNED_M
+    matched = bool(match) and match[M_sel]["z"] <= 1.0
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     out = torch.empty((H, W, 4), device="cuda", dtype=torch.float32)
@@ -653,58 +703,71 @@ def run_gpu(args):
 
     if rank != 0:
         return
-    # ---- CPU baseline and the per-pixel counts of the roofline ----
+    # ---- CPU baseline (the same learned form, full 1080p frames) and the roofline's counts ----
     peak, peak_kind = _peaks()
     cpu, lpc = None, None
+    threads = os.cpu_count() or 1
     if not args.no_cpu:
-        threads = os.cpu_count() or 1
-        fps_cpu, t_cpu, cw, ch, per_px, lpc = cpu_sample(args, threads, learned=(M_sel, net_params, net_box))
-        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": threads, "kind": "port",
-               "sample": f"oracle, plain form, frame 1 (temporal+spatial) at {cw}x{ch} ({t_cpu:.2f} s), scaled by pixel count to {W}x{H}"}
+        ct = _oracle_frames(args, threads, True, M_sel, 1, 3)
+        med = float(np.median(ct))
+        cpu = {"value": 1.0 / med, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": (f"oracle on {threads} host threads, learned form (M={M_sel}, FP16 bricks, 64 host Adam steps per frame), "
+                          f"median of 3 full {W}x{H} frames after 1 untimed"),
+               "ms_per_frame": [1000.0 * t for t in ct]}
+        lpc = roofline_counts(args, threads, M_sel, net_params, net_box)
     dom = max(("k_lp_generate", "k_net_infer", "k_lp_select", "spatial_final", "training"), key=lambda k: kernel_ms[k] or 0.0)
     roof, roof_tc = None, None
     if lpc is not None and kernel_ms["k_lp_generate"]:
         vox_bytes = 2
         per_px = lpc["generate_voxel_reads_px"] * vox_bytes + generate_stream_bytes_per_pixel(M_sel, lpc["vertices_px"], lpc["queries_px"])
+        survey_px = lpc["generate_voxel_reads_px"] * vox_bytes + SURVEY_STREAM_PX
         alg = per_px * W * H
         achieved = alg / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
+        achieved_s = survey_px * W * H / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": _traffic_from_profile("k_lp_generate"),
-                "kernel": "k_lp_generate + k_lp_bounce (the generate stage: one per-pixel launch, then one launch per bounce)",
+                "kernel": "the generate stage (features, primary distance rounds, first vertices, and per bounce a sort, the walks and the vertices)",
                 "peak_source": peak_kind,
                 "dominant_by_time": dom, "algorithmic_bytes_per_launch": alg, "algorithmic_bytes_per_pixel": per_px,
                 "voxel_reads_per_pixel": lpc["generate_voxel_reads_px"], "vertex_records_per_pixel": lpc["vertices_px"],
                 "queries_per_pixel": lpc["queries_px"], "kernel_ms": kernel_ms["k_lp_generate"],
-                "counts_from": f"oracle, learned form, frame 1 at {args.width // 4}x{args.height // 4}"}
+                "counts_from": f"oracle, learned form, frame 1 at {lpc['counted_at']}",
+                "stream_and_voxel_only": {"bytes_per_pixel": survey_px, "achieved": achieved_s, "frac": achieved_s / peak,
+                                          "definition": "voxel reads x 2 B + the plain path's reservoir/feature stream bytes "
+                                                        f"({SURVEY_STREAM_PX} B per pixel), without this design's own vertex, "
+                                                        "query and queue records"}}
     if kernel_ms["k_net_infer"]:
         tf = queries * NET_FLOP_PER_QUERY / (kernel_ms["k_net_infer"] / 1000.0) / 1e12
         pk = _bf16_peak()
         roof_tc = {"bound": "tensor", "kernel": "k_net_infer", "achieved": tf, "peak": pk[0], "unit": "TFLOP/s",
                    "frac": tf / pk[0] if pk[0] else None, "peak_source": pk[1], "queries_per_frame": queries,
                    "flop_per_query": NET_FLOP_PER_QUERY, "kernel_ms": kernel_ms["k_net_infer"]}
+    mt = match.get(M_sel, {})
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (bf16 MLP, fp16 bricks)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "width": W, "height": H, "max_path_length": opts.mMaxBounces,
-                       "candidates": M_sel, "spatial_samples": opts.mSpatialSampleCount, "bricks": "fp16",
-                       "l2": "inputs larger than L2 (bricks + reservoir buffers), no flush",
-                       "parallelism": f"replicas x{ws}", "volume_build_s": round(build_s, 2),
-                       "samples_per_s": value * W * H * (M_sel + opts.mSpatialSampleCount + 1),
-                       "kernel_ms": kernel_ms,
-                       "training": {"samples_per_frame": opts.mLearnedTrainSamples, "batch": opts.mLearnedBatch,
-                                    "lr": opts.mLearnedLearningRate}},
-            "plain": {"value": plain_fps, "unit": "frames/s", "candidates": 32, "bricks": "fp32",
-                      "kernel_ms": {"k_initial": kmsp[0], "k_spatial": kmsp[1]}, "speedup_learned_vs_plain": value / plain_fps,
-                      "bc4": {"value": bc4_fps, "unit": "frames/s", "frames": bc4_steps, "kernel_ms": {"k_initial": kmsb[0], "k_spatial": kmsb[1]},
-                              "bricks": "mip 0 fp32; coarse and conservative mips BC4", "relmse": rel.get("plain_bc4")}},
-            "relmse": {"matched": matched, "criterion": "learned - plain <= 2 standard errors of the difference",
-                       "plain": rel.get("plain"), "learned": rel.get(f"learned_M{M_sel}"),
-                       "all": {k: {"mean": v[0], "se": v[1]} for k, v in rel.items()}, **qinfo},
+            "relmse_summary": {"matched": matched, "learned": mt.get("relmse"), "plain": float(rel["plain"].mean()) if rel else None,
+                               "z": mt.get("z"), "candidates": M_sel, "equal_relmse_candidates": m_equal},
+            "plain_value": plain_fps, "speedup_learned_vs_plain": value / plain_fps,
+            "config": _config(args, M_sel, ws),
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": int(h2d.value), "d2h_bytes_per_step": int(d2h.value)},
             "gpu_launches": launches,
             "roofline": roof,
             "roofline_tensor": roof_tc,
             "cpu_baseline": cpu,
+            "details": {"volume_build_s": round(build_s, 2), "samples_per_s": value * W * H * (M_sel + opts.mSpatialSampleCount + 1),
+                        "kernel_ms": kernel_ms,
+                        "training": {"samples_per_frame": opts.mLearnedTrainSamples, "batch": opts.mLearnedBatch,
+                                     "lr": opts.mLearnedLearningRate}},
+            "plain": {"value": plain_fps, "unit": "frames/s", "candidates": 32, "bricks": "fp32",
+                      "kernel_ms": {"k_initial": kmsp[0], "k_spatial": kmsp[1]},
+                      "bc4": {"value": bc4_fps, "unit": "frames/s", "frames": bc4_steps, "kernel_ms": {"k_initial": kmsb[0], "k_spatial": kmsb[1]},
+                              "bricks": "mip 0 fp32; coarse and conservative mips BC4",
+                              "relmse": float(rel["plain_bc4"].mean()) if rel else None}},
+            "relmse": {"matched": matched, "criterion": "mean per-frame relMSE difference (learned - plain) <= 1 standard error",
+                       "plain": float(rel["plain"].mean()) if rel else None,
+                       "sweep": {str(k): v for k, v in match.items()}, "equal_relmse_candidates": m_equal,
+                       "plain_fp16": float(rel["plain_fp16"].mean()) if rel else None, **qinfo},
             "batched": batched,
             "small_configs": small,
             "animated": animated,
@@ -721,7 +784,8 @@ def main():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-quality", action="store_true", help="skip the relMSE matching (learned form at M=32)")
+    ap.add_argument("--no-quality", action="store_true", help="skip the relMSE matching sweep")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0, help="reference arm: seconds of timed frames at most")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched 32-instance form")
     ap.add_argument("--no-small", action="store_true", help="skip the 256^2 configurations (cfg1, cfg3, cfg4)")
     ap.add_argument("--no-animated", action="store_true", help="skip the animated-volume measurement")
