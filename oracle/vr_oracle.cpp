@@ -1464,11 +1464,12 @@ const int kLpValid = 1, kLpNeedsT = 2;
 
 // ComputeInitialSample with the shadow ray of the next-event estimate deferred to the network
 // and every resampling uniform drawn up front (the random stream does not depend on T).  The
-// first vertex draws from the pixel's stream; the indirect vertices (bounces >= 1) draw from the
-// candidate's own stream, seeded by (pixel, frame, candidate), so that they can be generated as
-// queued work apart from the other candidates.
-static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf, float preTr, Rng& sgPixel, LpVertex* rec, f3* extra,
-                                    float* queries /* [maxBounces][8] */, int px, int py, int frame, int cid) {
+// primary distance sample comes from the pixel's stream (the rounds of TraceRays, all drawn
+// before any vertex); every vertex, and the candidate's resampling uniform right after the first
+// vertex (ucOut), draws from the candidate's own stream, seeded by (pixel, frame, candidate), so
+// that candidates and their indirect vertices can be generated as work apart from the others.
+static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf, float preTr, LpVertex* rec, f3* extra,
+                                    float* queries /* [maxBounces][8] */, int px, int py, int frame, int cid, float* ucOut) {
     const Scene& sc = *c.sc;
     const SamplingOptions& options = c.initial;
     const int maxBounces = c.maxBounces;
@@ -1477,11 +1478,8 @@ static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf,
     const f3 sigma_s = sc.med.sigma_s, sigma_a = sc.med.sigma_a;
     const float sigma_t = sc.med.sigma_t;
     int bounce = 0;
-    Rng candidate{};
+    Rng sg = rng_create((uint32_t)px, (uint32_t)py, 0x40000000u | (((uint32_t)frame * 4096u + (uint32_t)cid) & 0x3FFFFFFFu));
     for (; bounce < maxBounces; bounce++) {
-        if (bounce == 1)
-            candidate = rng_create((uint32_t)px, (uint32_t)py, 0x40000000u | (((uint32_t)frame * 4096u + (uint32_t)cid) & 0x3FFFFFFFu));
-        Rng& sg = bounce == 0 ? sgPixel : candidate;
         Reservoir out = createNewReservoir();
         out.M = 1;
         float curHitDist, pdfDist = 0, Tr;
@@ -1591,6 +1589,7 @@ static float ComputeInitialSampleLP(Ctx& c, Ray ray, float preHit, float prePdf,
         }
         const float ub = maxBounces > 1 ? next1D(sg) : 0.f;
         rec[bounce] = LpVertex{out.runningSum, out.p_y, out.lightUV[0], out.lightUV[1], out.lightID, out.sampledPixel, flags, ub};
+        if (bounce == 0) *ucOut = next1D(sg);        // the candidate's resampling uniform
         if (hitEmpty) { bounce++; break; }
     }
     for (int b = bounce; b < maxBounces; ++b) { rec[b].flags = 0; queries[b * 8 + 6] = -1.f; }
@@ -1973,21 +1972,27 @@ struct Oracle {
             Ctx cl = c;
             std::vector<LpVertex> rec((size_t)M * mb);
             std::vector<f3> ex((size_t)M * std::max(mb - 1, 1));
-            std::vector<float> crec((size_t)M * 2), q((size_t)mb * 8);
+            std::vector<float> crec((size_t)M * 2), q((size_t)mb * 8), dist((size_t)M * 3);
             for (int x = 0; x < W; ++x) {
                 Rng sg = rng_create((uint32_t)x, (uint32_t)y, (uint32_t)(numTotalRounds * frameCount));
                 const size_t pid = (size_t)y * W + x;
                 Ray ray{cam.posW, normalize(rayDirPinhole(cam, x, y, W, H)), 0.f, kRayTMax};
-                int rounds = (M + 3) / 4, cid = 0;
-                for (int roundId = 0; roundId < rounds; roundId++) {
+                // the rounds of primary distance samples from the pixel's stream, then each
+                // candidate's vertices from its own stream
+                int rounds = (M + 3) / 4;
+                for (int roundId = 0, cid = 0; roundId < rounds; roundId++) {
                     float hd[4] = {0, 0, 0, 0}, pd[4] = {0, 0, 0, 0}, trs[4] = {0, 0, 0, 0};
                     int rs = roundId == rounds - 1 ? (M - 4 * (rounds - 1)) : 4;
                     SampleMediumAnalyticGeneric(sc, ray, sg, c.initial.visibilityUseLinearSampler, hd, c.initial.visibilityMipLevel, pd, trs, rs);
-                    for (int sid = 0; sid < rs; sid++, cid++) {
-                        float depth = ComputeInitialSampleLP(cl, ray, hd[sid], pd[sid], trs[sid], sg, &rec[(size_t)cid * mb],
-                                                             &ex[(size_t)cid * std::max(mb - 1, 1)], q.data(), x, y, frameCount, cid);
+                    for (int sid = 0; sid < rs; sid++, cid++) { dist[cid * 3] = hd[sid]; dist[cid * 3 + 1] = pd[sid]; dist[cid * 3 + 2] = trs[sid]; }
+                }
+                {
+                    for (int cid = 0; cid < M; ++cid) {
+                        float uc = 0.f;
+                        float depth = ComputeInitialSampleLP(cl, ray, dist[cid * 3], dist[cid * 3 + 1], dist[cid * 3 + 2], &rec[(size_t)cid * mb],
+                                                             &ex[(size_t)cid * std::max(mb - 1, 1)], q.data(), x, y, frameCount, cid, &uc);
                         crec[cid * 2] = depth;
-                        crec[cid * 2 + 1] = next1D(sg);
+                        crec[cid * 2 + 1] = uc;
                         int nv = 0;
                         for (int b = 0; b < mb; ++b) nv += (rec[(size_t)cid * mb + b].flags & kLpValid) ? 1 : 0;
                         lpVertices += nv;

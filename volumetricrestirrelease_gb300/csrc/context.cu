@@ -354,7 +354,7 @@ static int alloc_buffers(vr_context* c) {
 
 // ---- learned target: network state and the buffers of the split initial pass ----
 static void free_lp(vr_context* c) {
-    cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.ex); cudaFree(c->lp.T);
+    cudaFree(c->lp.vrecA); cudaFree(c->lp.vrecB); cudaFree(c->lp.crec); cudaFree(c->lp.dist); cudaFree(c->lp.ex); cudaFree(c->lp.T);
     cudaFree(c->lp.query); cudaFree(c->lp.qlist); cudaFree(c->lp.qcount); cudaFree(c->lp.rng); cudaFree(c->lp.train);
     cudaFree(c->lp.paths[0]); cudaFree(c->lp.paths[1]); cudaFree(c->lp.pcount); cudaFree(c->lp.psort); cudaFree(c->lp.hist);
     c->lp = vrd::LpBuffers{};
@@ -468,6 +468,7 @@ static int lp_alloc(vr_context* c) {
         c->lp.vrecA = dalloc<float4>(slots);
         c->lp.vrecB = dalloc<int4>(slots);
         c->lp.crec = dalloc<float2>((size_t)M * N);
+        c->lp.dist = dalloc<float4>((size_t)M * N);
         c->lp.ex = dalloc<float4>((size_t)M * std::max(MB - 1, 1) * N);
         c->lp.T = dalloc<float>(slots);
         c->lp.query = dalloc<float4>(2 * slots);
@@ -483,7 +484,7 @@ static int lp_alloc(vr_context* c) {
         c->lp.psort = dalloc<float4>(4 * paths);
         c->lp.hist = dalloc<int>(2 * vrd::kPathKeys);
         c->lp.pcount = dalloc<int>(16);         // queue lengths [0, MB], walk cursors from 8 on
-        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train ||
+        if (!c->lp.vrecA || !c->lp.vrecB || !c->lp.crec || !c->lp.dist || !c->lp.ex || !c->lp.T || !c->lp.query || !c->lp.qlist || !c->lp.qcount || !c->lp.rng || !c->lp.train ||
             !c->lp.paths[0] || !c->lp.paths[1] || !c->lp.pcount || !c->lp.psort || !c->lp.hist) {
             free_lp(c);
             c->err = "out of device memory (learned-target buffers)";

@@ -40,6 +40,7 @@ struct LpBuffers {
     float4* vrecA;     // [M * MB][N]: runningSum (or p_src), p_y (or unoccluded p_hat), uv0, uv1
     int4* vrecB;       // [M * MB][N]: lightID, sampledPixel, flags, resampling uniform (bits)
     float2* crec;      // [M][N]: depth, candidate resampling uniform
+    float4* dist;      // [M][N]: the candidate's primary distance sample: hit distance, pdf, Tr
     float4* ex;        // [M * (MB - 1)][N]: encoded direction / distance of each indirect vertex
     float* T;          // [M * MB][N]: predicted transmittance of the vertices with kLpNeedsT
     float4* query;     // [M * MB][N][2]: the query of each slot with kLpNeedsT: (x, y, z, wx), (wy, wz, tmax, slot bits)
