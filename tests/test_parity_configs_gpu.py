@@ -232,15 +232,17 @@ def _block_means(vlib, cuda, ctx, cam, frames, blocks):
 
 
 def _scores(a_blocks, b_blocks):
-    """Per-pixel error of mean(a) - mean(b) over its standard error (mean of the squares), the
-    image-average difference over its standard error, and the image-average relative difference.
-    Pixels where both estimates are constant (the background, seen unattenuated) are scored
-    against a floor of 1e-6 of the value."""
+    """Per-pixel error of mean(a) - mean(b) over its standard error (mean of the squares, over
+    the pixels where either estimate varies), the image-average difference over its standard
+    error, and the image-average relative difference.  Pixels where neither estimate varies
+    (the background seen unattenuated) must agree to float rounding instead (1e-5 relative)."""
     ma, mb = a_blocks.mean(0), b_blocks.mean(0)
     va = a_blocks.var(0, ddof=1) / len(a_blocks)
     vb = b_blocks.var(0, ddof=1) / len(b_blocks)
-    se = np.sqrt(va + vb) + 1e-6 * np.abs(mb) + 1e-12
-    z = (ma - mb) / se
+    varies = (va + vb) > 0
+    fixed = ~varies
+    assert np.all(np.abs(ma - mb)[fixed] <= 1e-5 * np.abs(mb)[fixed] + 1e-9), "constant pixels differ"
+    z = (ma - mb)[varies] / np.sqrt(va + vb)[varies]
     ga, gb = a_blocks.mean(axis=(1, 2, 3)), b_blocks.mean(axis=(1, 2, 3))
     gz = (ga.mean() - gb.mean()) / np.sqrt(ga.var(ddof=1) / len(ga) + gb.var(ddof=1) / len(gb))
     return float(np.mean(z ** 2)), float(gz), float((ga.mean() - gb.mean()) / gb.mean())
