@@ -454,16 +454,34 @@ def run_batched(args, lib):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.batch_steps
     px = sum(sc.width * sc.height for sc in descs)
+    launches = b.last_launch_count()
+    del b
+    # the same instances rendered one after another, each by its own vr_render_frame (the
+    # alternative to batching)
+    fs = f + args.batch_steps
+    for k in range(2):
+        for r, sc, o in zip(rends, descs, ptrs):
+            r.execute(sc.camera(fs + k), o)
+    torch.cuda.synchronize()
+    e0.record()
+    for k in range(2, 2 + args.batch_steps):
+        for r, sc, o in zip(rends, descs, ptrs):
+            r.execute(sc.camera(fs + k), o)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1) / args.batch_steps
     res = {"workload": "32 instances (8 fire plumes), resolutions from {256^2, 512^2, 960x540, 1280x720, 1920x1080}, "
                        "128^3..512^3 sparse fBm, max path length 3, 16..32 candidates, temporal + spatial, FP16 bricks, "
                        "learned target (2^15 training samples per instance and frame)",
            "instances": len(descs), "pixels_per_frame": px, "ms_per_batch_frame": ms, "batch_frames_per_s": 1000.0 / ms,
            "pixels_per_s": px * 1000.0 / ms, "equivalent_1080p_frames_per_s": px * 1000.0 / ms / (1920 * 1080),
-           "graph": True, "launches_per_frame": b.last_launch_count(),
+           "sequential": {"ms_per_frame": ms_seq, "pixels_per_s": px * 1000.0 / ms_seq,
+                          "what": "the 32 instances rendered one after another with vr_render_frame"},
+           "speedup_vs_sequential": ms_seq / ms,
+           "graph": True, "launches_per_frame": launches,
            "autotune": {"chosen_tile": f"{shape[0]}x{shape[1]}", "blocks_per_sm": shape[2], "trial_ms": trials,
                         "candidates": "tiles 8x16, 16x8, 32x4 x 5, 3, 8 blocks per SM (first trials)"},
            "volume_build_s": round(build_s, 1), "timed_frames": args.batch_steps}
-    del b
     return res
 
 

@@ -27,8 +27,14 @@ void VR_CAT(launch_batch_pass_, VR_MB)(const vrd::BatchLaunch& BL, int pass, int
         default: vrd::kb_pixels<VR_MB, vrd::kPassFinal><<<grid, 128, 0, st>>>(BL); break;
     }
 }
-void VR_CAT(launch_batch_lp_bounce_, VR_MB)(const vrd::BatchLaunch& BL, int inst, int b, int grid, cudaStream_t st) {
-    vrd::kb_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(BL, inst, b);
+// walk: point-sampled distances (the instance's initial visibility sampler), as resumable walks
+void VR_CAT(launch_batch_lp_bounce_, VR_MB)(const vrd::BatchLaunch& BL, int inst, int b, int grid, int walk, cudaStream_t st) {
+    if (walk) {
+        vrd::kb_lp_walk<VR_MB><<<grid, 128, 0, st>>>(BL, inst, b);
+        vrd::kb_lp_vertex<VR_MB><<<grid, 128, 0, st>>>(BL, inst, b);
+    } else {
+        vrd::kb_lp_bounce<VR_MB><<<grid, 128, 0, st>>>(BL, inst, b);
+    }
 }
 void VR_CAT(launch_batch_train_gen_, VR_MB)(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
     vrd::kb_train_gen<VR_MB><<<grid, 128, 0, st>>>(BL);

@@ -37,7 +37,8 @@ namespace vrk {
 #define VR_DECL(MB)                                                                                           \
     cudaError_t upload_scene_##MB(const vrd::DevScene&, cudaStream_t);                                         \
     void launch_initial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, dim3, dim3, cudaStream_t);     \
-    void launch_spatial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::SpatialParams&, dim3, dim3, cudaStream_t); \
+    void launch_spatial_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::SpatialParams&, dim3, dim3, const vrd::SpatialSplit*, int, \
+                             cudaStream_t);                                                                     \
     void launch_final_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, int, dim3, dim3, cudaStream_t);  \
     void launch_reference_##MB(const vrd::FrameParams&, int, int, double*, dim3, dim3, cudaStream_t);        \
     void launch_lp_generate_##MB(const vrd::FrameParams&, const vrd::FrameBuffers&, const vrd::LpBuffers&, dim3, dim3, cudaStream_t); \
@@ -308,6 +309,8 @@ struct vr_context {
     float netBmin[3] = {0, 0, 0}, netBinv[3] = {1, 1, 1};
     int numSMs = 0;
     vrd::LpBuffers lp{};
+    vrd::SpatialSplit split{};           // buffers of the split spatial round (allocated when used)
+    size_t splitSlots = 0;
     size_t lpSlots = 0;            // allocated vertex slots (M * MB * N)
     int lpM = 0, lpMB = 0;
     float* stepLoss = nullptr;     // loss of each Adam step of the last frame
@@ -349,6 +352,39 @@ static int alloc_buffers(vr_context* c) {
     if (!c->color) { c->err = "out of device memory (colour)"; return VR_ERR_OOM; }
     cudaMemset(c->color, 0, N * 4 * sizeof(float));
     c->allocMB = mb; c->allocW = c->W; c->allocH = c->H;
+    return VR_OK;
+}
+
+// ---- the split spatial round: recorded segments, their transmittances, the p-hat table ----
+static void free_split(vr_context* c) {
+    cudaFree(c->split.seg); cudaFree(c->split.tr); cudaFree(c->split.list); cudaFree(c->split.counts); cudaFree(c->split.E);
+    c->split = vrd::SpatialSplit{};
+    c->splitSlots = 0;
+}
+// the spatial options take the split round (vrd::spatialSplitEligible, from the options)
+static bool split_needed(const vr_context* c) {
+    const vr_options& o = c->opts;
+    return o.mEnableSpatialReuse && !o.mUseReference && o.mSpatialSampleCount <= vrd::kSplitK &&
+           o.mSpatialVisibilityTrackingMethod == VR_TRACK_RAY_MARCHING && o.mSpatialLightingTrackingMethod == VR_TRACK_RAY_MARCHING;
+}
+static int split_alloc(vr_context* c) {
+    const size_t N = (size_t)c->W * c->H;
+    const size_t slots = N * (size_t)(vrd::kSplitK * vrd::kSplitK) * (size_t)(c->opts.mMaxBounces + 1);
+    if (c->split.seg && c->splitSlots == slots) return VR_OK;
+    free_split(c);
+    if (slots > (size_t)INT32_MAX) { c->err = "image too large for the split spatial round"; return VR_ERR_INVALID_ARG; }
+    c->split.seg = dalloc<float4>(2 * slots);
+    c->split.tr = dalloc<float>(slots);
+    c->split.list = dalloc<uint2>(slots);
+    c->split.counts = dalloc<int>(2);
+    c->split.E = dalloc<float>(N * vrd::kSplitK * vrd::kSplitK);
+    if (!c->split.seg || !c->split.tr || !c->split.list || !c->split.counts || !c->split.E) {
+        free_split(c);
+        c->err = "out of device memory (split spatial round)";
+        return VR_ERR_OOM;
+    }
+    c->split.capacity = (int)slots;
+    c->splitSlots = slots;
     return VR_OK;
 }
 
@@ -773,6 +809,9 @@ vr_context* vr_create(const vr_options* opts, int32_t width, int32_t height, int
     vr_context* c = new vr_context();
     c->opts = *opts;
     c->W = width; c->H = height;
+    // persistent grids (walks, marches, network kernels) are sized by the SM count
+    cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, dev);
+    if (c->numSMs <= 0) c->numSMs = 1;
     for (auto& e : c->ev) cudaEventCreate(&e);
     if (dev_malloc(&c->status, sizeof(int)) != cudaSuccess) { delete c; if (err) *err = VR_ERR_OOM; return nullptr; }
     cudaMemset(c->status, 0, sizeof(int));
@@ -785,6 +824,7 @@ void vr_destroy(vr_context* c) {
     if (!c) return;
     free_buffers(c);
     free_lp(c);
+    free_split(c);
     free_net(c);
     for (void* p : c->sceneAllocs) cudaFree(p);
     for (void* p : c->envAllocs) cudaFree(p);
@@ -1210,6 +1250,7 @@ static int prepare_frame(vr_context* c, const vr_camera* cam) {
     int r = alloc_buffers(c);
     if (r) return r;
     if (lp_active(c) && (r = lp_alloc(c))) return r;
+    if (split_needed(c) && (r = split_alloc(c))) return r;
     if (c->optionsChanged) { c->frameCount = 0; c->temporalSampleAccumulated = 0; c->optionsChanged = false; }
     return VR_OK;
 }
@@ -1617,11 +1658,12 @@ static void launch_initial(const vrd::FrameParams& P, const vrd::FrameBuffers& B
     else vrk::launch_initial_4(P, B, g, b, st);
 }
 template <int MB>
-static void launch_spatial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st) {
-    if (MB == 1) vrk::launch_spatial_1(P, B, S, g, b, st);
-    else if (MB == 2) vrk::launch_spatial_2(P, B, S, g, b, st);
-    else if (MB == 3) vrk::launch_spatial_3(P, B, S, g, b, st);
-    else vrk::launch_spatial_4(P, B, S, g, b, st);
+static void launch_spatial(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b,
+                           const vrd::SpatialSplit* SS, int persistent, cudaStream_t st) {
+    if (MB == 1) vrk::launch_spatial_1(P, B, S, g, b, SS, persistent, st);
+    else if (MB == 2) vrk::launch_spatial_2(P, B, S, g, b, SS, persistent, st);
+    else if (MB == 3) vrk::launch_spatial_3(P, B, S, g, b, SS, persistent, st);
+    else vrk::launch_spatial_4(P, B, S, g, b, SS, persistent, st);
 }
 template <int MB>
 static void launch_final(const vrd::FrameParams& P, const vrd::FrameBuffers& B, int wh, dim3 g, dim3 b, cudaStream_t st) {
@@ -1784,7 +1826,8 @@ static void launch_frame_kernels(vr_context* c, const vrd::FrameParams& P, vrd::
             int r2 = ((o.mSpatialReuseRounds + 1) * c->frameCount + r) % 16;
             neighbor_offsets(o, r2, S.offs);
             VR_RANGE("vr.spatial");
-            launch_spatial<MB>(P, B, S, grid, block, st);
+            launch_spatial<MB>(P, B, S, grid, block, c->split.seg ? &c->split : nullptr, c->numSMs * VR_KINIT_MIN_BLOCKS, st);
+            if (c->split.seg && vrd::spatialSplitEligible(P)) c->launches += 4;
             VR_RANGE_END();
             c->launches++;
             totalRoundId++;
@@ -2000,7 +2043,7 @@ namespace vrk {
 #define VR_BDECL(MB)                                                                      \
     void launch_batch_pass_##MB(const vrd::BatchLaunch&, int, int, cudaStream_t);       \
     void launch_batch_train_gen_##MB(const vrd::BatchLaunch&, int, cudaStream_t);        \
-    void launch_batch_lp_bounce_##MB(const vrd::BatchLaunch&, int, int, int, cudaStream_t);
+    void launch_batch_lp_bounce_##MB(const vrd::BatchLaunch&, int, int, int, int, cudaStream_t);
 VR_BDECL(1) VR_BDECL(2) VR_BDECL(3) VR_BDECL(4)
 #undef VR_BDECL
 }  // namespace vrk
@@ -2049,11 +2092,11 @@ static void batch_pass(const vrd::BatchLaunch& BL, int pass, int grid, cudaStrea
     else vrk::launch_batch_pass_4(BL, pass, grid, st);
 }
 template <int MB>
-static void batch_lp_bounce(const vrd::BatchLaunch& BL, int inst, int bounce, int grid, cudaStream_t st) {
-    if (MB == 1) vrk::launch_batch_lp_bounce_1(BL, inst, bounce, grid, st);
-    else if (MB == 2) vrk::launch_batch_lp_bounce_2(BL, inst, bounce, grid, st);
-    else if (MB == 3) vrk::launch_batch_lp_bounce_3(BL, inst, bounce, grid, st);
-    else vrk::launch_batch_lp_bounce_4(BL, inst, bounce, grid, st);
+static void batch_lp_bounce(const vrd::BatchLaunch& BL, int inst, int bounce, int grid, int walk, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_lp_bounce_1(BL, inst, bounce, grid, walk, st);
+    else if (MB == 2) vrk::launch_batch_lp_bounce_2(BL, inst, bounce, grid, walk, st);
+    else if (MB == 3) vrk::launch_batch_lp_bounce_3(BL, inst, bounce, grid, walk, st);
+    else vrk::launch_batch_lp_bounce_4(BL, inst, bounce, grid, walk, st);
 }
 template <int MB>
 static void batch_train_gen(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
@@ -2201,8 +2244,9 @@ static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
         for (int i = 0; i < n; ++i)
             if (lp_active(b->ctx[i]))
                 for (int bn = 1; bn < MB; ++bn) {
-                    batch_lp_bounce<MB>(BL, i, bn, grid, st);
-                    launches++;
+                    const int walk = b->ctx[i]->opts.mInitialVisibilityUseLinearSampler ? 0 : 1;
+                    batch_lp_bounce<MB>(BL, i, bn, grid, walk, st);
+                    launches += 1 + walk;
                 }
         for (vr_context* c : b->ctx)
             if (lp_active(c)) {

@@ -20,8 +20,21 @@ cudaError_t VR_CAT(upload_scene_, VR_MB)(const vrd::DevScene& s, cudaStream_t st
 void VR_CAT(launch_initial_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, dim3 g, dim3 b, cudaStream_t st) {
     vrd::k_initial<VR_MB><<<g, b, 0, st>>>(P, B);
 }
-void VR_CAT(launch_spatial_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b, cudaStream_t st) {
-    vrd::k_spatial<VR_MB><<<g, b, 0, st>>>(P, B, S);
+void VR_CAT(launch_spatial_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::SpatialParams& S, dim3 g, dim3 b,
+                                    const vrd::SpatialSplit* SS, int persistent, cudaStream_t st) {
+    // the round with its marches split out when its options allow (the same result); else
+    // the per-thread round
+    if (SS && vrd::spatialSplitEligible(P)) {
+        cudaMemsetAsync(SS->counts, 0, 2 * sizeof(int), st);
+        vrd::k_split_a<VR_MB><<<g, b, 0, st>>>(P, B, S, *SS);
+        vrd::k_split_march<<<persistent, 128, 0, st>>>(*SS);
+        cudaMemsetAsync(SS->counts, 0, 2 * sizeof(int), st);
+        vrd::k_split_b<VR_MB><<<g, b, 0, st>>>(P, B, S, *SS);
+        vrd::k_split_march<<<persistent, 128, 0, st>>>(*SS);
+        vrd::k_split_c<VR_MB><<<g, b, 0, st>>>(P, B, S, *SS);
+    } else {
+        vrd::k_spatial<VR_MB><<<g, b, 0, st>>>(P, B, S);
+    }
 }
 void VR_CAT(launch_final_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, int writeHist, dim3 g, dim3 b, cudaStream_t st) {
     vrd::k_final<VR_MB><<<g, b, 0, st>>>(P, B, writeHist);

@@ -81,6 +81,31 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_lp_bounce(const B
         lpBouncePath<MB>(sP, sL, b, sL.paths[b & 1], i);
 }
 
+// the bounce pass b of learned instance `inst` as resumable walks over its queue, then the
+// vertices (point-sampled distances; see k_lp_walk)
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_lp_walk(const BatchLaunch BL, int inst, int b) {
+    __shared__ FrameParams sP;
+    __shared__ LpBuffers sL;
+    const BatchInstance& I = BL.inst[inst];
+    blockCopy(&c_scene, I.scene);
+    blockCopy(&sP, &I.P);
+    blockCopy(&sL, &I.L);
+    __syncthreads();
+    lpWalkPass<MB>(sP, sL, b, sL.paths[b & 1]);
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) kb_lp_vertex(const BatchLaunch BL, int inst, int b) {
+    __shared__ FrameParams sP;
+    __shared__ LpBuffers sL;
+    const BatchInstance& I = BL.inst[inst];
+    blockCopy(&c_scene, I.scene);
+    blockCopy(&sP, &I.P);
+    blockCopy(&sL, &I.L);
+    __syncthreads();
+    lpVertexPass<MB>(sP, sL, b, sL.paths[b & 1]);
+}
+
 // training samples of every learned instance, in chunks of 128 that never straddle instances
 template <int MB>
 __global__ void __launch_bounds__(128) kb_train_gen(const BatchLaunch BL) {

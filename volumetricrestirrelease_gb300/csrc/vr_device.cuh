@@ -863,6 +863,133 @@ __device__ inline float trRayMarch(const Ray& r, int mip, bool lin, float tss, v
     trackVolume(r, mip, sg, a, false);
     return a.Tr;
 }
+// ---------------------------------------------------------------------------------------
+// Resumable ray-marched transmittance: the walk of trackVolume + TrRayMarch (cell-centred) as
+// explicit state advanced one tree node or one trip of the march (up to two samples) per call,
+// for kernels in which a lane whose march ends takes new work while the rest of its warp goes
+// on marching.  Performs the operations of trRayMarch in the same order.
+// ---------------------------------------------------------------------------------------
+struct MarchWalk {
+    HDDA dda;
+    f3 p, wpt, vmin;
+    float tNear, tFar, t, Tr, tStep;
+    float tMax1, tMax2;
+    int lev, node, nid1, brick, oiter, iter;
+    bool inBrick, lin;
+};
+__device__ __forceinline__ void marchAscend(const DevSlot& s, MarchWalk& w) {
+    const float kVdel[3] = {1.f, 8.f, 128.f};
+    while (w.lev <= 2 && w.dda.t.x > (w.lev == 1 ? w.tMax1 : w.tMax2)) {
+        w.lev++;
+        if (w.lev <= 2) {
+            w.node = w.lev == 1 ? w.nid1 : 0;
+            w.vmin = nodeVmin(s, w.lev, w.node);
+            w.dda.prepare(w.vmin, kVdel[w.lev]);
+        }
+    }
+}
+// set-up of a march along rWorld in slot `mip` (the tStep of trRayMarch); false when it ended
+// there (w.Tr = 1: the ray misses the volume)
+__device__ __forceinline__ bool marchStart(const DevSlot& s, int mip, const Ray& rWorld, float tStep, bool lin, MarchWalk& w) {
+    Ray ray;
+    ray.o = mulPoint(rWorld.o, s.M);
+    ray.d = mulVec(rWorld.d, s.M);
+    ray.tMin = rWorld.tMin; ray.tMax = rWorld.tMax;
+    w.Tr = 0.f;
+    w.tStep = tStep;
+    w.lin = lin;
+    float tNear, tFar;
+    if (!intersectBound(ray, tNear, tFar, mip, false)) { w.Tr = 1.f; return false; }
+    w.tNear = tNear;
+    w.tFar = tFar;
+    f3 tStart = mk3(tNear, tFar, 0);
+    w.vmin = mk3(0.f);
+    w.node = 0;
+    tStart.x += 0.01f;
+    w.tMax2 = tStart.y;
+    w.dda.setFromRay(ray.o, ray.d, tStart);
+    w.dda.prepare(w.vmin, 128.f);
+    w.t = tNear;
+    w.lev = 2;
+    w.oiter = 0;
+    w.inBrick = false;
+    return true;
+}
+// one step; true when the march has ended (w.Tr holds the transmittance)
+__device__ __forceinline__ bool marchStep(const DevSlot& s, int mip, MarchWalk& w) {
+    const float eps = 0.01f;
+    if (w.inBrick) {
+        // one trip of TrRayMarch::mainStep's loop
+        if (!(w.iter < kMaxBrickSteps && inLeafF(w.p))) {
+            w.inBrick = false;
+            w.dda.step();
+            w.dda.t.x += eps;
+            marchAscend(s, w);
+            w.oiter++;
+            return false;
+        }
+        if (w.t >= w.tFar) { w.Tr = vr::exp_(w.Tr); return true; }
+        const float mult = 1.f;
+        const f3 p1 = w.p + w.wpt;
+        const float t1 = w.t + mult * w.tStep;
+        const bool second = w.iter + 1 < kMaxBrickSteps && inLeafF(p1) && !(t1 >= w.tFar);
+        const float d0 = densityLocal(mip, w.brick, w.p, w.lin);
+        const float d1 = second ? densityLocal(mip, w.brick, p1, w.lin) : 0.f;
+        float sigma_t = d0 * c_scene.sigma_t;
+        w.Tr += -sigma_t * (w.iter == 0 ? 1.f : mult) * w.tStep;
+        w.p = p1;
+        w.t = t1;
+        w.iter++;
+        if (!second) return false;
+        sigma_t = d1 * c_scene.sigma_t;
+        w.Tr += -sigma_t * mult * w.tStep;
+        w.p = w.p + w.wpt;
+        w.t += mult * w.tStep;
+        w.iter++;
+        return false;
+    }
+    const int kDim[3] = {3, 4, 5}, kRes[3] = {8, 16, 32};
+    const float kVdel[3] = {1.f, 8.f, 128.f};
+    const int* q = w.dda.p;
+    if (!(w.oiter < 4096 && w.lev > 0 && w.lev <= 2 && q[0] >= 0 && q[1] >= 0 && q[2] >= 0 && q[0] <= kRes[w.lev] && q[1] <= kRes[w.lev] &&
+          q[2] <= kRes[w.lev])) {
+        w.Tr = vr::exp_(w.Tr);
+        return true;
+    }
+    w.dda.next();
+    const int b = (((w.dda.p[2] << kDim[w.lev]) + w.dda.p[1]) << kDim[w.lev]) + w.dda.p[0];
+    const int child = getChild(s, w.node, w.lev, b);
+    if (child >= 0) {
+        if (w.lev == 1) {
+            w.t = w.dda.t.x - eps;
+            if (w.t >= w.tFar) { w.Tr = vr::exp_(w.Tr); return true; }
+            const f3 vl = nodeVmin(s, 0, child);
+            // TrRayMarch::mainStep's entry: the first sample point of the brick
+            w.t = w.tNear + (vr::floor_((w.t - w.tNear) / w.tStep) + 0.5f) * w.tStep;
+            if (w.t < w.dda.t.x) w.t += w.tStep;
+            const f3 wp = w.dda.pos + w.t * w.dda.dir;
+            w.p = wp - vl;
+            w.wpt = 1.f * w.tStep * w.dda.dir;
+            w.iter = 0;
+            w.brick = child;
+            w.inBrick = true;
+            return false;
+        }
+        w.lev--;
+        w.nid1 = child;
+        w.node = child;
+        w.vmin = nodeVmin(s, w.lev, child);
+        w.tMax1 = w.dda.t.y;
+        w.dda.prepare(w.vmin, kVdel[w.lev]);
+    } else {
+        w.dda.step();
+        w.dda.t.x += eps;
+    }
+    marchAscend(s, w);
+    w.oiter++;
+    return false;
+}
+
 __device__ inline float trResidual(const Ray& r, int mip, vr::Rng& sg, bool analog, bool global) {
     ResidualRatio a; a.analog = analog || global; a.global = global;
     trackVolume(r, mip, sg, a, false);
@@ -1079,8 +1206,16 @@ __device__ inline f3 sampleDirectLighting(vr::Rng& sg, float& pdf, const MediumI
 // ---------------------------------------------------------------------------------------
 // path contribution re-evaluation (ReSTIRHelper.slang:91-496)
 // ---------------------------------------------------------------------------------------
+// Where evaluateF takes its transmittances from: DirectVis estimates them in place; the split
+// spatial round records the segments first and replays the marched values (k_spatial_split).
+struct DirectVis {
+    __device__ __forceinline__ float operator()(const Ray& r, vr::Rng& sg, int samples, int mip, bool lin, uint32_t method, float tss) {
+        return computeVisibility(r, sg, samples, mip, lin, method, tss);
+    }
+};
+template <class V>
 __device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, float uv0, float uv1, vr::Rng& sg, const SamplingOptions& o, bool cull,
-                                       int off) {
+                                       int off, V& vis) {
     Ray sr;
     f3 Ld;
     if (lid < 0) {
@@ -1095,15 +1230,16 @@ __device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, flo
     } else {
         return mk3(0.f);
     }
-    float Tr = computeVisibility(sr, sg, o.lightSamples, cull ? o.lightingMipLevel + off : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
+    float Tr = vis(sr, sg, o.lightSamples, cull ? o.lightingMipLevel + off : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
     return Tr * Ld;
 }
 
 // extra: the extra-bounce plane base, indexed extra[b * N + tap.startPixel]; lastFrame: the
 // sample as of the previous frame (the temporal tap's MIS weight), on the previous animation
 // frame's grids when the volume is animated and usePrevGrid is set
-static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* extra, int N, Ray ray, vr::Rng& sg, const SamplingOptions& o,
-                               int maxBounces, bool noReuse, bool isFinal, bool lastFrame = false) {
+template <class V>
+static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4* extra, int N, Ray ray, vr::Rng& sg, const SamplingOptions& o,
+                                             int maxBounces, bool noReuse, bool isFinal, bool lastFrame, V& vis) {
     const bool useLast = lastFrame && c_scene.usePrevGrid && c_scene.hasAnimation;
     const int off = useLast ? kPrevSlotOffset : 0;
     bool isBg = tap.depth == kRayTMax;
@@ -1118,7 +1254,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
         float density = (isBg || noReuse) ? 1.f : densityWorld(pW, off);
         if (density == 0.f) return mk3(0.f);
         if (!noReuse)
-            visibility = computeVisibility(ray, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
+            visibility = vis(ray, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
         f3 sig = isBg ? mk3(1.f) : (isSelfEmission ? c_scene.sigma_a : c_scene.sigma_s);
         if (noReuse && !isBg) sig = sig / c_scene.sigma_t;
         F = F * (visibility * density * sig);
@@ -1168,7 +1304,7 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
                     if (vr::all_eq0(F)) return mk3(0.f);
                     float sv = 1.f;
                     if (!noReuse)
-                        sv = computeVisibility(sr, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
+                        sv = vis(sr, sg, o.visibilitySamples, o.visibilityMipLevel + off, o.visibilityUseLinearSampler != 0, o.visibilityTrackingMethod, o.visibilityTStepScale);
                     F = F * sv;
                     mi.wo = -sr.d;
                     mi.p = pW;
@@ -1178,10 +1314,15 @@ static __device__ __noinline__ f3 evaluateF(const Reservoir& tap, const float4* 
                 else mi = MediumInteraction{at(sr, sr.tMax), -sr.d, c_scene.g, true};
             }
             if (!scatterEm && vr::any_gt0(F))
-                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal, off);
+                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal, off, vis);
         }
     }
     return F;
+}
+__device__ __forceinline__ f3 evaluateF(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o,
+                                        int maxBounces, bool noReuse, bool isFinal, bool lastFrame = false) {
+    DirectVis v;
+    return evaluateFV<DirectVis>(tap, extra, N, ray, sg, o, maxBounces, noReuse, isFinal, lastFrame, v);
 }
 __device__ __forceinline__ float evalPHat(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o, int mb,
                                          bool lastFrame = false) {

@@ -524,6 +524,279 @@ __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_spatial(const __gr
     spatialPixel<MB>(P, B, S, px, py);
 }
 
+// ---------------------------------------------------------------------------------------
+// The SpatialReuse round with its marches split out (the default spatial options: ray-marched
+// visibility and light transmittance, one sample each, at most kSplitK taps).
+//
+// Per pixel the round re-evaluates p-hat up to K^2 - K times, and each evaluation marches the
+// camera segment, every suffix segment and the light segment; per thread, the lanes of a warp
+// wait for the longest march of every evaluation.  Here the evaluations run twice through
+// evaluateFV: first recording the segments they would march (RecordVis, which answers 1 and
+// lists the segment), then, after k_split_march has marched every listed segment as resumable
+// walks (a lane whose march ends takes the next segment), replaying the marched values
+// (ReplayVis).  Transmittance only scales F, so a recording walks the same branches as the
+// replay or further, never fewer; the replay consumes a prefix of the recorded segments in the
+// same order and evaluates exactly what evaluateF does.  Three per-pixel kernels:
+//   k_split_a : records E(s, 0) (each neighbour tap at this pixel's ray, resampleNeighbor)
+//               and, for Talbot MIS, E(0, j) (the centre's reservoir at every tap's ray);
+//   k_split_b : replays them into E, and records E(s, j) for the taps with weight left;
+//   k_split_c : the round itself (SpatialReuse.cs.slang:94-264), E(s, j) replayed in place,
+//               then the history copy and the final shading of the last round.
+// ---------------------------------------------------------------------------------------
+constexpr int kSplitK = 4;
+struct SpatialSplit {
+    float4* seg;        // [slots][2]: (origin, tMax), (direction, march step) of each recorded segment
+    float* tr;          // [slots]: its marched transmittance
+    uint2* list;        // recorded segments: (slot, mip | linear << 8)
+    int* counts;        // [0] entries in list, [1] next entry of the marches
+    float* E;           // [N][kSplitK * kSplitK]: p-hat of tap s at pixel j's ray
+    int capacity;       // entries of list
+};
+__device__ __forceinline__ size_t splitSlot(int pid, int s, int j, int MB) {
+    return ((size_t)pid * (kSplitK * kSplitK) + (size_t)(s * kSplitK + j)) * (size_t)(MB + 1);
+}
+struct RecordVis {
+    const SpatialSplit* S;
+    size_t base;
+    int k;
+    __device__ float operator()(const Ray& r, vr::Rng&, int, int mip, bool lin, uint32_t, float tss) {
+        const size_t slot = base + (size_t)(k++);
+        // the march step of trRayMarch
+        int eff = mip >= kPrevSlotOffset ? mip - kPrevSlotOffset : mip;
+        eff = eff >= kNumMaxMips ? eff - kNumMaxMips : eff;
+        const float tStep = c_scene.tStep * tss * (float)(eff + 1);
+        S->seg[2 * slot] = make_float4(r.o.x, r.o.y, r.o.z, r.tMax);
+        S->seg[2 * slot + 1] = make_float4(r.d.x, r.d.y, r.d.z, tStep);
+        const unsigned m = __activemask();
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int b = 0;
+        if (lane == leader) b = atomicAdd(S->counts, __popc(m));
+        b = __shfl_sync(m, b, leader) + __popc(m & ((1u << lane) - 1u));
+        if (b < S->capacity) S->list[b] = make_uint2((uint32_t)slot, (uint32_t)mip | (lin ? 256u : 0u));
+        else if (c_scene.status) atomicOr(c_scene.status, 2);
+        return 1.f;
+    }
+};
+struct ReplayVis {
+    const float* tr;
+    size_t base;
+    int k;
+    // computeVisibility's average over its samples, with the marched values
+    __device__ float operator()(const Ray&, vr::Rng&, int samples, int, bool, uint32_t, float) {
+        float vis = 0;
+        for (int i = 0; i < samples; i++) vis += tr[base + (size_t)k];
+        k++;
+        vis /= samples;
+        return vis;
+    }
+};
+__host__ __device__ inline bool spatialSplitEligible(const FrameParams& P) {
+    return P.spatialK <= kSplitK && P.spatial.visibilityTrackingMethod == VR_TRACK_RAY_MARCHING &&
+           P.spatial.lightingTrackingMethod == VR_TRACK_RAY_MARCHING && P.spatial.visibilitySamples == 1 && P.spatial.lightSamples == 1;
+}
+
+__device__ __forceinline__ bool splitPixel(const FrameParams& P, int& px, int& py) {
+    px = blockIdx.x * 8 + (threadIdx.x & 7);
+    py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
+    return px < P.W && py < P.H;
+}
+
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_a(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (!splitPixel(P, px, py)) return;
+    const int W = P.W, H = P.H, N = P.N, K = P.spatialK;
+    const int pid = py * W + px;
+    if (__ldg(&B.featCur[pid]) == 1.f) return;
+    const ResBuf& in = B.sp[S.in];
+    const Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H)), 0, kRayTMax};
+    vr::Rng unused;
+    for (int s = P.spatialTalbot ? 0 : 1; s < K; s++) {
+        const int tx = px + S.offs[s][0], ty = py + S.offs[s][1];
+        if (!(tx >= 0 && tx < W && ty >= 0 && ty < H)) continue;
+        const Reservoir tap = loadRes(in, ty * W + tx);
+        if (s > 0 && tap.runningSum != 0.f) {
+            RecordVis v{&SS, splitSlot(pid, s, 0, MB), 0};
+            evaluateFV(tap, in.extra, N, ray, unused, P.spatial, MB, false, false, false, v);
+        }
+        if (s == 0 && P.spatialTalbot && tap.runningSum > 0.f) {
+            for (int j = 1; j < K; j++) {
+                const int tx2 = px + S.offs[j][0], ty2 = py + S.offs[j][1];
+                if (!(tx2 >= 0 && tx2 < W && ty2 >= 0 && ty2 < H)) continue;
+                const Ray nr{ray.o, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, tx2, ty2, W, H)), 0, tap.depth};
+                RecordVis v{&SS, splitSlot(pid, 0, j, MB), 0};
+                evaluateFV(tap, in.extra, N, nr, unused, P.spatial, MB, false, false, false, v);
+            }
+        }
+    }
+}
+
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_b(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (!splitPixel(P, px, py)) return;
+    const int W = P.W, H = P.H, N = P.N, K = P.spatialK;
+    const int pid = py * W + px;
+    if (__ldg(&B.featCur[pid]) == 1.f) return;
+    const ResBuf& in = B.sp[S.in];
+    const Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H)), 0, kRayTMax};
+    vr::Rng unused;
+    for (int s = P.spatialTalbot ? 0 : 1; s < K; s++) {
+        const int tx = px + S.offs[s][0], ty = py + S.offs[s][1];
+        if (!(tx >= 0 && tx < W && ty >= 0 && ty < H)) continue;
+        const Reservoir tap = loadRes(in, ty * W + tx);
+        float rs = tap.runningSum;
+        if (s > 0 && tap.runningSum != 0.f) {
+            ReplayVis v{SS.tr, splitSlot(pid, s, 0, MB), 0};
+            const float ph = vr::luminance(evaluateFV(tap, in.extra, N, ray, unused, P.spatial, MB, false, false, false, v));
+            SS.E[(size_t)pid * (kSplitK * kSplitK) + s * kSplitK] = ph;
+            float w = ph / tap.p_y;
+            if (vr::isinf_(w) || vr::isnan_(w)) w = 0.f;
+            rs = tap.runningSum * w;
+        }
+        if (!P.spatialTalbot || !(rs > 0.f)) continue;
+        for (int j = 1; j < K; j++) {
+            if (j == s) continue;
+            const int tx2 = px + S.offs[j][0], ty2 = py + S.offs[j][1];
+            if (!(tx2 >= 0 && tx2 < W && ty2 >= 0 && ty2 < H)) continue;
+            const Ray nr{ray.o, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, tx2, ty2, W, H)), 0, tap.depth};
+            if (s == 0) {
+                ReplayVis v{SS.tr, splitSlot(pid, 0, j, MB), 0};
+                SS.E[(size_t)pid * (kSplitK * kSplitK) + j] =
+                    vr::luminance(evaluateFV(tap, in.extra, N, nr, unused, P.spatial, MB, false, false, false, v));
+            } else {
+                RecordVis v{&SS, splitSlot(pid, s, j, MB), 0};
+                evaluateFV(tap, in.extra, N, nr, unused, P.spatial, MB, false, false, false, v);
+            }
+        }
+    }
+}
+
+// the recorded segments, marched as resumable walks
+static __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_split_march(const __grid_constant__ SpatialSplit SS) {
+    const int n = min(SS.counts[0], SS.capacity);
+    const int lane = threadIdx.x & 31;
+    MarchWalk w;
+    uint32_t slot = 0;
+    int mip = 0;
+    bool live = false, exhausted = false;
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !live && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(SS.counts + 1, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!live && !exhausted) {
+                const int idx = base + __popc(need & ((1u << lane) - 1u));
+                if (idx >= n) exhausted = true;
+                else {
+                    const uint2 e = SS.list[idx];
+                    slot = e.x;
+                    mip = (int)(e.y & 255u);
+                    const float4 a = SS.seg[2 * (size_t)slot], d = SS.seg[2 * (size_t)slot + 1];
+                    const Ray r{mk3(a.x, a.y, a.z), mk3(d.x, d.y, d.z), 0.f, a.w};
+                    live = marchStart(c_scene.slots[mip], mip, r, d.w, (e.y & 256u) != 0, w);
+                    if (!live) SS.tr[slot] = w.Tr;
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, live) == 0) {
+            if (__ballot_sync(0xffffffffu, !exhausted) == 0) break;
+            continue;
+        }
+        if (live && marchStep(c_scene.slots[mip], mip, w)) {
+            SS.tr[slot] = w.Tr;
+            live = false;
+        }
+    }
+}
+
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_c(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (!splitPixel(P, px, py)) return;
+    const int W = P.W, H = P.H, N = P.N;
+    const int pid = py * W + px;
+    const ResBuf& in = B.sp[S.in];
+    const ResBuf& outb = B.sp[S.out];
+    const float* E = SS.E + (size_t)pid * (kSplitK * kSplitK);
+    vr::Rng sg = vr::rng_create((uint32_t)px, (uint32_t)py, (uint32_t)(S.numRounds * P.frameCount + S.rid));
+    Reservoir output = loadRes(in, pid);
+    const int centerStart = pid;
+    const Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, H)), 0, kRayTMax};
+    if (P.spatialTalbot) output = newReservoir();
+    bool hasSel = output.runningSum > 0.f;
+    Reservoir result;
+    if (__ldg(&B.featCur[pid]) == 1.f) {
+        result = P.spatialTalbot ? loadRes(in, pid) : output;
+        storeRes(outb, pid, result);
+        if (MB > 1) {
+            int mib = decodeBounces(output.sampledPixel, MB);
+            for (int b = 0; b < mib; b++) outb.extra[(size_t)b * N + output.startPixel] = __ldg(&in.extra[(size_t)b * N + output.startPixel]);
+        }
+        result.startPixel = pid;
+    } else {
+        const int K = P.spatialK;
+        vr::Rng unused;
+        for (int s = P.spatialTalbot ? 0 : 1; s < K; s++) {
+            int tx = px + S.offs[s][0], ty = py + S.offs[s][1];
+            if (!(tx >= 0 && tx < W && ty >= 0 && ty < H)) continue;
+            Reservoir tap = loadRes(in, ty * W + tx);
+            float mis = 1.f;
+            if (s > 0 && tap.runningSum != 0.f) {          // resampleNeighbor, p-hat from k_split_b
+                const float ph = E[s * kSplitK];
+                float w = ph / tap.p_y;
+                if (vr::isinf_(w) || vr::isnan_(w)) w = 0.f;
+                tap.runningSum *= w;
+                tap.p_y = ph;
+            }
+            if (P.spatialTalbot && tap.runningSum > 0.f) {
+                float p_sum = 0, p_qi = 0, k = 0;
+                for (int j = 0; j < K; j++) {
+                    int tx2 = px + S.offs[j][0], ty2 = py + S.offs[j][1];
+                    if (!(tx2 >= 0 && tx2 < W && ty2 >= 0 && ty2 < H)) continue;
+                    float4 a2 = __ldg(&in.a[ty2 * W + tx2]);
+                    float M2 = a2.y;
+                    k += M2;
+                    if (j == 0) { p_qi = tap.p_y; p_sum += tap.p_y * M2; }
+                    else if (s == j) { p_qi = a2.w; p_sum += a2.w * M2; }
+                    else {
+                        float p_y;
+                        if (s == 0) p_y = E[j];
+                        else {
+                            Ray nr{ray.o, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, tx2, ty2, W, H)), 0, tap.depth};
+                            ReplayVis v{SS.tr, splitSlot(pid, s, j, MB), 0};
+                            p_y = vr::luminance(evaluateFV(tap, in.extra, N, nr, unused, P.spatial, MB, false, false, false, v));
+                        }
+                        if (vr::isinf_(p_y) || vr::isnan_(p_y)) p_y = 0.f;
+                        p_sum += p_y * M2;
+                    }
+                }
+                if (p_sum > 0) mis = p_qi * k / p_sum;
+            }
+            tap.runningSum *= mis;
+            if (resampleStep(tap, output, sg)) hasSel = true;
+        }
+        if (MB > 1) {
+            if (hasSel) {
+                int mib = decodeBounces(output.sampledPixel, MB);
+                for (int b = 0; b < mib; b++) outb.extra[(size_t)b * N + centerStart] = __ldg(&in.extra[(size_t)b * N + output.startPixel]);
+            }
+            output.startPixel = centerStart;
+        }
+        storeRes(outb, pid, output);
+        result = output;
+    }
+    if (S.last) {
+        if (S.writeHistory) writeHistory<MB>(B, outb, result, pid, N);
+        finalShade<MB>(P, B, outb, result, px, py);
+    }
+}
+
 // k_final: FinalShading without spatial reuse (optionally after the history copy)
 template <int MB>
 __device__ __forceinline__ void finalPixel(const FrameParams& P, const FrameBuffers& B, int writeHist, int px, int py) {

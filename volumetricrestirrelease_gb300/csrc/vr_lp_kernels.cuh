@@ -427,9 +427,10 @@ __device__ __forceinline__ bool lpWalkStep(const DevSlot& s, int mip, LpWalk& w)
     return false;
 }
 
-// the distance samples of the queue of bounce b (its sorted copy), written back into the entries
+// the distance samples of the queue of bounce b held in `queue` (a frame's sorted copy, or a
+// batched instance's queue itself), written back into its entries
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+__device__ __forceinline__ void lpWalkPass(const FrameParams& P, const LpBuffers& L, int b, float4* queue) {
     const int n = min(L.pcount[b], L.pcapacity);
     const SamplingOptions& o = P.initial;
     int mip = o.visibilityMipLevel;
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __gr
                 if (idx >= n) exhausted = true;
                 else {
                     w.entry = (size_t)idx;
-                    const float4* q = L.psort + 4 * w.entry;
+                    const float4* q = queue + 4 * w.entry;
                     const float4 q0 = q[0], q1 = q[1], q3 = q[3];
                     w.g.s[0] = __float_as_uint(q3.x); w.g.s[1] = __float_as_uint(q3.y);
                     w.g.s[2] = __float_as_uint(q3.z); w.g.s[3] = __float_as_uint(q3.w);
@@ -459,7 +460,7 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __gr
                     live = true;
                     if (!lpWalkStart(s, mip, r, w)) live = false, exhausted = false;
                     if (!live) {
-                        float4* qw = L.psort + 4 * w.entry;
+                        float4* qw = queue + 4 * w.entry;
                         qw[0].w *= w.pdf; qw[1].w *= w.tr; qw[2].z = w.hit;
                         qw[3] = make_float4(__uint_as_float(w.g.s[0]), __uint_as_float(w.g.s[1]), __uint_as_float(w.g.s[2]), __uint_as_float(w.g.s[3]));
                     }
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __gr
             continue;
         }
         if (live && lpWalkStep(s, mip, w)) {
-            float4* qw = L.psort + 4 * w.entry;
+            float4* qw = queue + 4 * w.entry;
             qw[0].w *= w.pdf; qw[1].w *= w.tr; qw[2].z = w.hit;
             qw[3] = make_float4(__uint_as_float(w.g.s[0]), __uint_as_float(w.g.s[1]), __uint_as_float(w.g.s[2]), __uint_as_float(w.g.s[3]));
             live = false;
@@ -479,12 +480,17 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __gr
     }
 }
 
-// the vertices of the queue of bounce b from the distances k_lp_walk left in its entries
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_walk(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+    lpWalkPass<MB>(P, L, b, L.psort);
+}
+
+// the vertices of the queue of bounce b from the distances the walks left in its entries
+template <int MB>
+__device__ __forceinline__ void lpVertexPass(const FrameParams& P, const LpBuffers& L, int b, const float4* queue) {
     const int n = min(L.pcount[b], L.pcapacity);
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < (size_t)n; i += (size_t)gridDim.x * blockDim.x) {
-        const float4* q = L.psort + 4 * i;
+        const float4* q = queue + 4 * i;
         const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3];
         LpPath cs;
         cs.ray = Ray{mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), 0.f, kRayTMax};
@@ -495,6 +501,10 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex(const __
         // pdf and Tr are already in pathPdf and pathPHat: x * 1 = x
         if (lpVertex<MB>(P, cs, q2.z, 1.f, 1.f, g, L, c, pid)) lpEnqueue(L, b + 1, cs, pid, c, g);
     }
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L, int b) {
+    lpVertexPass<MB>(P, L, b, L.psort);
 }
 
 // Counting sort of a queue by coherence key before its bounce pass: the octant of the direction
@@ -672,5 +682,6 @@ __global__ void __launch_bounds__(128) k_lp_train_gen(const __grid_constant__ Fr
     if (i >= L.trainCount) return;
     lpTrainSample<MB>(P, L, seed, i);
 }
+
 
 }  // namespace vrd
