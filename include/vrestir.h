@@ -61,8 +61,8 @@ extern "C" {
 #define VR_BRICK_APRON 10           /* stored brick edge: 8 + 2 x apron of 1 */
 
 /* Options: same names, meanings and defaults as VolumetricReSTIRParams
- * (VolumetricReSTIR.h:130-207).  Members absent here (surface scenes, vertex reuse, mesh
- * lights, animation) are outside this path.  vr_options_default() fills the defaults. */
+ * (VolumetricReSTIR.h:130-207).  Members absent here (surface scenes, mesh lights) are outside
+ * this path; animation is set with vr_set_animation.  vr_options_default() fills the defaults. */
 typedef struct vr_options {
     int32_t mMaxBounces;                        /* 1 */
     int32_t mEnableTemporalReuse;               /* 1 */
@@ -122,6 +122,13 @@ typedef struct vr_options {
     /* animated volumes (VolumetricReSTIR.h:152): evaluate the temporal tap's MIS weight on the
      * previous animation frame's grids (VolumeDesc.usePrevGridForReproj) */
     int32_t mUsePrevVolumeForReproj;            /* 1 */
+    /* vertex reuse (VolumetricReSTIR.h:136-137, the VERTEX_REUSE define): from indirect vertex
+     * mVertexReuseStartBounce on, a path's suffix is kept as vertex positions, so spatial reuse
+     * reconnects the shifted prefix to the same suffix vertex and reuses the suffix's share of
+     * p_hat (p_partial) instead of re-marching it.  Needs mMaxBounces > 1; not with the learned
+     * target, batches or the allocation-free frame. */
+    int32_t mVertexReuse;                       /* 0 */
+    int32_t mVertexReuseStartBounce;            /* 1 */
 } vr_options;
 
 /* Participating medium (Scene.cpp:3246-3262 VolumeDesc + addGVDBVolume arguments). */
@@ -206,7 +213,8 @@ typedef struct vr_camera {        /* Camera.cpp:183-189 pinhole frame, no jitter
 } vr_camera;
 
 /* AoS reservoir record exactly as HostDeviceSharedDefinitions.h:16-45 lays it out
- * (32 bytes for max path length 1; 36 bytes with extraBounceStartId otherwise). */
+ * (32 bytes for max path length 1; 36 bytes with extraBounceStartId otherwise; 40 bytes with
+ * p_partial as well under vertex reuse). */
 typedef struct vr_reservoir_aos {
     float runningSum;
     float M;
@@ -216,6 +224,7 @@ typedef struct vr_reservoir_aos {
     int32_t lightID;
     int32_t sampledPixel;
     int32_t extraBounceStartId;   /* present in the exported stream only if mMaxBounces > 1 */
+    float p_partial;              /* present only with mVertexReuse and mMaxBounces > 1 */
 } vr_reservoir_aos;
 
 typedef struct vr_context vr_context;

@@ -220,8 +220,8 @@ class Oracle:
         return out.reshape(-1, 8) if which in (0, 2) else out
 
     def export_reservoirs(self, which=0):
-        from volumetricrestirrelease_gb300.restir import RESERVOIR_DTYPE_36
-        out = np.zeros(self.width * self.height, RESERVOIR_DTYPE_36)
+        from volumetricrestirrelease_gb300.restir import RESERVOIR_DTYPE_40
+        out = np.zeros(self.width * self.height, RESERVOIR_DTYPE_40)
         self.L.vro_export_reservoirs(self._h, which, _ptr(out))
         return out
 
@@ -268,7 +268,7 @@ OPTION_DEFAULTS = dict(
     mSpatialSampleCount=4, mSpatialMISMethod=1, mFinalLightSamples=1, mFinalVisibilitySamples=1,
     mFinalVisibilityTrackingMethod=1, mFinalLightTrackingMethod=1, mFinalTStepScale=0.2, mUseLearnedPHat=0,
     mLearnedTrainSamples=1 << 20, mLearnedBatch=16384, mLearnedLearningRate=1e-3, mLearnedTFloor=0.02, mLearnedSeed=1,
-    mLearnedTargetMethod=2, mLearnedLoss=0, mUsePrevVolumeForReproj=1)
+    mLearnedTargetMethod=2, mLearnedLoss=0, mUsePrevVolumeForReproj=1, mVertexReuse=0, mVertexReuseStartBounce=1)
 
 
 def default_options(**overrides):

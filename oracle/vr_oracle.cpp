@@ -57,12 +57,14 @@ struct Reservoir {
     float runningSum, M, depth, p_y;
     float lightUV[2];
     int lightID, sampledPixel, extraBounceStartId;
+    float p_partial;            // vertex reuse: the suffix's share of p_hat (HostDeviceSharedDefinitions.h:29-31)
 };
 static Reservoir createNewReservoir() {                 // Reservoir.slang:19-23
     Reservoir r;
     r.runningSum = 0.f; r.M = 0.f; r.depth = FLT_MAX; r.p_y = 0.f;
     r.lightUV[0] = 0.f; r.lightUV[1] = 0.f; r.lightID = 0; r.sampledPixel = 0;
     r.extraBounceStartId = 0;
+    r.p_partial = 0.f;
     return r;
 }
 static void copySample(const Reservoir& from, Reservoir& to) {
@@ -70,6 +72,7 @@ static void copySample(const Reservoir& from, Reservoir& to) {
     to.lightUV[0] = from.lightUV[0]; to.lightUV[1] = from.lightUV[1];
     to.lightID = from.lightID; to.extraBounceStartId = from.extraBounceStartId;
     to.sampledPixel = from.sampledPixel;
+    to.p_partial = from.p_partial;          // Reservoir.slang:46-48, 76-78 (vertex reuse)
 }
 // Reservoir.slang:26-57
 static bool simpleResampleStep(const Reservoir& reservoir, Reservoir& state, Rng& sg) {
@@ -115,7 +118,11 @@ static void encodeEmissivePosition(f3 pos, int& lightID, float lightUV[2]) {
     lightID = asint(pos.z); lightUV[0] = pos.x; lightUV[1] = pos.y;
 }
 struct f4 { float x, y, z, w; };
-static f4 decodeWiDist(f3 input) {                        // reuseAsVertex == false
+static f4 decodeWiDist(f3 input, bool reuseAsVertex = false) {     // ReSTIRHelper.slang:21-39
+    if (reuseAsVertex) {
+        if (input.x == kRayTMax) return f4{0.f, 0.f, 0.f, kRayTMax};
+        return f4{input.x, input.y, input.z, -1.f};
+    }
     f3 wi;
     wi.x = input.x; wi.y = input.y;
     wi.z = sqrt_(1.0f - (input.x * input.x + input.y * input.y));
@@ -1111,6 +1118,7 @@ struct SamplingOptions {
     bool visibilityUseLinearSampler, lightingUseLinearSampler;
     float visibilityTStepScale, lightingTStepScale;
     bool useEnvironmentLights, useAnalyticLights;
+    int vertexReuseStartBounce = -1;        // vertex reuse (VERTEX_REUSE): first reconnection bounce; -1 off
 };
 
 struct Ctx {             // per-call constants
@@ -1184,6 +1192,12 @@ static Reservoir ComputeInitialSample(Ctx& c, Ray primaryRay, float preHit, floa
             mi.p = ray.at(curHitDist); mi.wo = -ray.dir; mi.g = sc.med.g; mi.isValid = curHitDist != kRayTMax;
         }
         pathPdf *= pdfDist;
+        const int vrs = options.vertexReuseStartBounce;
+        // ComputeInitialSample.slang:88-94: the reconnection vertex in area measure
+        if (vrs >= 0 && bounce == vrs && curHitDist != kRayTMax) {
+            pathPdf /= curHitDist * curHitDist;
+            pathPHat /= curHitDist * curHitDist;
+        }
         bool hitEmpty = false;
         float actualVolumeDensity = 0.f;
         if (bounce == 0) {
@@ -1195,7 +1209,9 @@ static Reservoir ComputeInitialSample(Ctx& c, Ray primaryRay, float preHit, floa
             out.depth = primaryScatterDepth;
             if (maxBounces > 1) {
                 out.sampledPixel = encodeMaxIndirectBounces(out.sampledPixel, bounce);
-                extra[bounce - 1] = encodeWiDist(ray.dir, !mi.isValid ? kRayTMax : curHitDist);
+                // ComputeInitialSample.slang:114-127: from the reuse bounce on, vertex positions
+                if (vrs >= 0 && bounce >= vrs) extra[bounce - 1] = !mi.isValid ? mk3(kRayTMax) : mi.p;
+                else extra[bounce - 1] = encodeWiDist(ray.dir, !mi.isValid ? kRayTMax : curHitDist);
             }
             out.p_y = pathPdf;
         }
@@ -1239,8 +1255,10 @@ static Reservoir ComputeInitialSample(Ctx& c, Ray primaryRay, float preHit, floa
                     if (out.runningSum > 0.f) {
                         out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
                         if (out.lightID == kSelfEmissionLightID && bounce > 0) {
-                            encodeEmissivePosition(mi.p, out.lightID, out.lightUV);
-                            p_y /= (curHitDist * curHitDist);
+                            if (vrs < 0 || bounce < vrs) {          // ComputeInitialSample.slang:322-330
+                                encodeEmissivePosition(mi.p, out.lightID, out.lightUV);
+                                p_y /= (curHitDist * curHitDist);
+                            }
                             out.sampledPixel = encodePathTag(out.sampledPixel, 1);
                         }
                         out.p_y = p_y;
@@ -1604,8 +1622,10 @@ struct ExtraProvider {        // StructuredBuffer/Array data providers (ArrayDat
     f3 get(int i) const { return data[i]; }
 };
 
+// precomputedVisibility / lightVisibilityReuse: vertex reuse (ReSTIRHelper.slang:443-496) takes the
+// light transmittance from the reservoir's p_partial, or hands the marched one back for it
 static f3 evaluate_L_in_volume(const Ctx& c, const MediumInteraction& mi, int lightID, const float lightUV[2], Rng& sg, const SamplingOptions& options, bool cullNonOpaque,
-                               int densityGridOffset) {
+                               int densityGridOffset, float* precomputedVisibility = nullptr, bool lightVisibilityReuse = false) {
     const Scene& sc = *c.sc;
     Ray shadowRay;
     f3 Ld = mk3(0.f);
@@ -1621,13 +1641,24 @@ static f3 evaluate_L_in_volume(const Ctx& c, const MediumInteraction& mi, int li
     } else {
         return mk3(0.f);      // mesh lights are outside this path
     }
-    float Tr = computeVisibility(sc, shadowRay, sg, options.lightSamples, cullNonOpaque ? options.lightingMipLevel + densityGridOffset : 0,
-                                 options.lightingUseLinearSampler, options.lightingTrackingMethod, options.lightingTStepScale);
+    float Tr;
+    if (lightVisibilityReuse) Tr = *precomputedVisibility;
+    else {
+        Tr = computeVisibility(sc, shadowRay, sg, options.lightSamples, cullNonOpaque ? options.lightingMipLevel + densityGridOffset : 0,
+                               options.lightingUseLinearSampler, options.lightingTrackingMethod, options.lightingTStepScale);
+        if (precomputedVisibility) *precomputedVisibility = Tr;
+    }
     return Tr * Ld;
 }
 
+// spatialReuse and pPartialOut: vertex reuse (ReSTIRHelper.slang:91-420; the reservoir is REUSETYPE
+// inout there): spatial reuse takes the suffix's share of p_hat from tap.p_partial; other calls
+// write the share they evaluate to *pPartialOut (when given)
 static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, Ray ray, Rng& sg, const SamplingOptions& options,
-                      bool noReuse, bool isFinalShading, bool isLastFrame = false) {
+                      bool noReuse, bool isFinalShading, bool isLastFrame = false, bool spatialReuse = false, float* pPartialOut = nullptr) {
+    const int vrs = options.vertexReuseStartBounce;
+    const bool vr = vrs >= 0;
+    f3 P_prefix = mk3(1.f);
     const Scene& sc = *c.sc;
     const bool useLastFrameGrid = sc.usePrevGrid && isLastFrame && sc.hasAnimation;
     const int mipLevelOffset = useLastFrameGrid ? kPrevSlotOffset : 0;
@@ -1665,8 +1696,8 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                 int numIndirectBounces = maxIndirectBounces;
                 for (; bounceId < numIndirectBounces; bounceId++) {
                     bool isCurrentVertexEmissive = isScatterSelfEmission && bounceId == numIndirectBounces - 1;
-                    f4 wiDist = decodeWiDist(extra.get(tap.extraBounceStartId + bounceId));
-                    if (isCurrentVertexEmissive) {
+                    f4 wiDist = decodeWiDist(extra.get(tap.extraBounceStartId + bounceId), vr && bounceId + 1 >= vrs);
+                    if (isCurrentVertexEmissive && (!vr || bounceId + 1 < vrs)) {
                         f3 pe = decodeEmissivePosition(tap.lightID, tap.lightUV);
                         wiDist.x = pe.x; wiDist.y = pe.y; wiDist.z = pe.z; wiDist.w = -1.f;
                     }
@@ -1683,6 +1714,10 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                     f3 bsdf = mk3(phaseFunction(mi, mi.wo, scatterRay.dir));
                     F = F * bsdf;
                     if (all_eq0(F)) return mk3(0.f);
+                    if (vr && bounceId == vrs) {                 // ReSTIRHelper.slang:289-295
+                        if (spatialReuse) return F * tap.p_partial;
+                        P_prefix = F;
+                    }
                     if (wiDist.w == -1.f) p_World = mk3(wiDist.x, wiDist.y, wiDist.z);
                     else p_World = scatterRay.at(scatterRay.tMax);
                     f3 sig; float scatterDensity;
@@ -1694,7 +1729,8 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                         scatterDensity = 1.f;
                     }
                     F = F * (scatterDensity * sig);
-                    if (isCurrentVertexEmissive) F = F * (1.f / (dist * dist));
+                    if (vr ? (bounceId + 1 == vrs || (isCurrentVertexEmissive && bounceId + 1 < vrs)) : isCurrentVertexEmissive)
+                        F = F * (1.f / (dist * dist));
                     if (all_eq0(F)) return mk3(0.f);
                     float scatterVisibility = 1.f;
                     if (!noReuse)
@@ -1708,20 +1744,30 @@ static f3 evaluate_F_(const Ctx& c, Reservoir tap, const ExtraProvider& extra, R
                 if (isScatterSelfEmission) F = F * EmissionWorldSpace(*c.sc, p_World, useLastFrameGrid);
                 else mi = MediumInteraction{scatterRay.at(scatterRay.tMax), -scatterRay.dir, sc.med.g, true};
             }
-            if (!isScatterSelfEmission && any_gt0(F))
-                F = F * evaluate_L_in_volume(c, mi, tap.lightID, tap.lightUV, sg, options, !isFinalShading, mipLevelOffset);
+            if (!isScatterSelfEmission && any_gt0(F)) {
+                const bool lightVisibilityReuse = vr && bounceId == vrs && spatialReuse;
+                float precomputedVisibility = tap.p_partial;
+                F = F * evaluate_L_in_volume(c, mi, tap.lightID, tap.lightUV, sg, options, !isFinalShading, mipLevelOffset, &precomputedVisibility,
+                                             lightVisibilityReuse);
+                if (vr && bounceId == vrs && !spatialReuse && pPartialOut) *pPartialOut = precomputedVisibility;
+            }
         }
     }
+    // ReSTIRHelper.slang:415-419: the suffix's share of p_hat
+    if (vr && bounceId > vrs && !spatialReuse && pPartialOut) *pPartialOut = luminance(F / P_prefix);
     return F;
 }
 static float evaluate_P_hat(const Ctx& c, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o, const Reservoir& tap,
-                            bool isLastFrame = false) {
-    f3 F = evaluate_F_(c, tap, extra, ray, sg, o, false, false, isLastFrame);
+                            bool isLastFrame = false, bool spatialReuse = false, float* pPartialOut = nullptr) {
+    f3 F = evaluate_F_(c, tap, extra, ray, sg, o, false, false, isLastFrame, spatialReuse, pPartialOut);
     return luminance(F);
 }
-static void resampleNeighbor(const Ctx& c, Reservoir& tap, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o) {
+// resampleNeighbor (spatialReuse false: the tap's p_partial is re-evaluated, the reservoir being
+// REUSETYPE inout) and resampleNeighborSpatialReuse (spatialReuse true), ReSTIRHelper.slang:567-600
+static void resampleNeighbor(const Ctx& c, Reservoir& tap, const Ray& ray, Rng& sg, const ExtraProvider& extra, const SamplingOptions& o,
+                             bool spatialReuse = false) {
     if (tap.runningSum == 0.f) return;
-    float p_y_hat = evaluate_P_hat(c, ray, sg, extra, o, tap);
+    float p_y_hat = evaluate_P_hat(c, ray, sg, extra, o, tap, false, spatialReuse, spatialReuse ? nullptr : &tap.p_partial);
     float weight = p_y_hat / tap.p_y;
     if (isinf_(weight) || isnan_(weight)) weight = 0.f;
     tap.runningSum *= weight;
@@ -1893,6 +1939,11 @@ struct Oracle {
         c.fin = SamplingOptions{o.mFinalVisibilityTrackingMethod, o.mFinalLightTrackingMethod, flA ? 1 : o.mFinalLightSamples, 0,
                                 fvA ? 1 : o.mFinalVisibilitySamples, 0, true, true, o.mFinalTStepScale, o.mFinalTStepScale,
                                 o.mUseEnvironmentLights != 0, o.mUseAnalyticLights != 0};
+        // VolumetricReSTIR.cpp:118-121, 376-386: the VERTEX_REUSE define, for paths with indirect vertices
+        const int vrs = (o.mVertexReuse && o.mMaxBounces > 1) ? o.mVertexReuseStartBounce : -1;
+        c.initial.vertexReuseStartBounce = vrs;
+        c.spatial.vertexReuseStartBounce = vrs;
+        c.fin.vertexReuseStartBounce = vrs;
     }
 
     // GenerateFeatures.cs.slang:57-101
@@ -1937,7 +1988,7 @@ struct Oracle {
                     }
                 }
                 ExtraProvider prov{finalExtra};
-                float p_hat = evaluate_P_hat(cl, ray, sg, prov, c.spatial, fin);
+                float p_hat = evaluate_P_hat(cl, ray, sg, prov, c.spatial, fin, false, false, &fin.p_partial);
                 if (fin.runningSum > 0.f) {
                     fin.runningSum *= fin.p_y == 0.f ? 0.f : p_hat / fin.p_y;
                     fin.p_y = p_hat;
@@ -2362,7 +2413,7 @@ struct Oracle {
                     if (!(tx >= 0 && tx < W && ty >= 0 && ty < H)) continue;
                     Reservoir tap = perPixel[in][(size_t)ty * W + tx];
                     float MISWeight = 1.f;
-                    if (sid > 0) resampleNeighbor(cl, tap, ray, sg, prov, cl.spatial);
+                    if (sid > 0) resampleNeighbor(cl, tap, ray, sg, prov, cl.spatial, true);
                     if (talbot && tap.runningSum > 0.f) {
                         float p_sum = 0, p_qi = 0, k = 0;
                         for (int j = 0; j < K; j++) {
@@ -2374,7 +2425,7 @@ struct Oracle {
                             else if (sid == j) { p_qi = tap2.p_y; p_sum += tap2.p_y * tap2.M; }
                             else {
                                 Ray nr{ray.origin, normalize(rayDirPinhole(cam, tx2, ty2, W, H)), 0, tap.depth};
-                                float p_y = evaluate_P_hat(cl, nr, sg, prov, cl.spatial, tap);
+                                float p_y = evaluate_P_hat(cl, nr, sg, prov, cl.spatial, tap, false, true);
                                 if (isinf_(p_y) || isnan_(p_y)) p_y = 0.f;
                                 p_sum += p_y * tap2.M;
                             }
@@ -2646,6 +2697,7 @@ int vro_export_reservoirs(void* h, int which, vr_reservoir_aos* out) {
         o.runningSum = r.runningSum; o.M = r.M; o.depth = r.depth; o.p_y = r.p_y;
         o.lightUV[0] = r.lightUV[0]; o.lightUV[1] = r.lightUV[1];
         o.lightID = r.lightID; o.sampledPixel = r.sampledPixel; o.extraBounceStartId = r.extraBounceStartId;
+        o.p_partial = r.p_partial;
     }
     return 0;
 }

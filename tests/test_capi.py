@@ -43,7 +43,7 @@ def test_default_options_match_reference(vlib):
 
 
 def test_struct_sizes_match_header():
-    assert C.sizeof(capi.ReservoirAoS) == 36
+    assert C.sizeof(capi.ReservoirAoS) == 40
     assert C.sizeof(capi.PointLight) == 24
     assert C.sizeof(capi.Camera) == 48
 

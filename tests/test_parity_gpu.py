@@ -44,10 +44,11 @@ def _compare_frame(gpu, ora, opts, cuda, cam, f, check_buffers=True):
     assert nbad == 0, f"frame {f}: {nbad} pixels differ from the oracle"
     if not check_buffers or opts.mUseReference:
         return img
+    vr = bool(opts.mVertexReuse) and opts.mMaxBounces > 1
     for which in (0, 1) if opts.mEnableTemporalReuse else (0,):
-        rg = as_reservoirs(gpu.export_reservoirs(which), opts.mMaxBounces)
+        rg = as_reservoirs(gpu.export_reservoirs(which), opts.mMaxBounces, vr)
         ro = ora.export_reservoirs(which)
-        for k in FIELDS:
+        for k in FIELDS + (("p_partial",) if vr else ()):
             assert _same(rg[k], ro[k]), f"frame {f} buffer {which}: reservoir field {k} differs"
         if opts.mMaxBounces > 1:
             # extra-bounce records are compared where a reservoir references them

@@ -45,6 +45,7 @@ class Options(C.Structure):
         ("mUseLearnedPHat", _i32), ("mLearnedTrainSamples", _i32), ("mLearnedBatch", _i32),
         ("mLearnedLearningRate", _f32), ("mLearnedTFloor", _f32), ("mLearnedSeed", _u32),
         ("mLearnedTargetMethod", _u32), ("mLearnedLoss", _i32), ("mUsePrevVolumeForReproj", _i32),
+        ("mVertexReuse", _i32), ("mVertexReuseStartBounce", _i32),
     ]
 
     def as_dict(self):
@@ -96,7 +97,7 @@ class Camera(C.Structure):
 
 class ReservoirAoS(C.Structure):
     _fields_ = [("runningSum", _f32), ("M", _f32), ("depth", _f32), ("p_y", _f32), ("lightUV", _f32 * 2),
-                ("lightID", _i32), ("sampledPixel", _i32), ("extraBounceStartId", _i32)]
+                ("lightID", _i32), ("sampledPixel", _i32), ("extraBounceStartId", _i32), ("p_partial", _f32)]
 
 
 # exported entry points and their signatures (include/vrestir.h)

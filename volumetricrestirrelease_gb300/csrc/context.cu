@@ -310,6 +310,7 @@ struct vr_context {
     int numSMs = 0;
     vrd::LpBuffers lp{};
     vrd::SpatialSplit split{};           // buffers of the split spatial round (allocated when used)
+    float* ppPlane[3] = {nullptr, nullptr, nullptr};   // p_partial of res[0..2], bound under vertex reuse
     size_t splitSlots = 0;
     size_t lpSlots = 0;            // allocated vertex slots (M * MB * N)
     int lpM = 0, lpMB = 0;
@@ -325,6 +326,7 @@ static void free_buffers(vr_context* c) {
     }
     cudaFree(c->feat[0]); cudaFree(c->feat[1]); cudaFree(c->color);
     c->feat[0] = c->feat[1] = nullptr; c->color = nullptr;
+    for (int i = 0; i < 3; ++i) { cudaFree(c->ppPlane[i]); c->ppPlane[i] = nullptr; }
     c->allocMB = 0;
 }
 
@@ -351,6 +353,11 @@ static int alloc_buffers(vr_context* c) {
     c->color = dalloc<float>(N * 4);
     if (!c->color) { c->err = "out of device memory (colour)"; return VR_ERR_OOM; }
     cudaMemset(c->color, 0, N * 4 * sizeof(float));
+    for (int i = 0; i < 3; ++i) {
+        c->ppPlane[i] = dalloc<float>(N);
+        if (!c->ppPlane[i]) { c->err = "out of device memory (p_partial)"; return VR_ERR_OOM; }
+        cudaMemset(c->ppPlane[i], 0, N * sizeof(float));
+    }
     c->allocMB = mb; c->allocW = c->W; c->allocH = c->H;
     return VR_OK;
 }
@@ -364,7 +371,7 @@ static void free_split(vr_context* c) {
 // the spatial options take the split round (vrd::spatialSplitEligible, from the options)
 static bool split_needed(const vr_context* c) {
     const vr_options& o = c->opts;
-    return o.mEnableSpatialReuse && !o.mUseReference && o.mSpatialSampleCount <= vrd::kSplitK &&
+    return o.mEnableSpatialReuse && !o.mUseReference && !(o.mVertexReuse && o.mMaxBounces > 1) && o.mSpatialSampleCount <= vrd::kSplitK &&
            o.mSpatialVisibilityTrackingMethod == VR_TRACK_RAY_MARCHING && o.mSpatialLightingTrackingMethod == VR_TRACK_RAY_MARCHING;
 }
 static int split_alloc(vr_context* c) {
@@ -485,6 +492,9 @@ static vrd::NetView net_view(const vr_context* c) {
     return v;
 }
 
+// vertex reuse in effect: the option, and paths with indirect vertices
+static bool vertex_reuse(const vr_context* c) { return c->opts.mVertexReuse && c->opts.mMaxBounces > 1; }
+
 static bool lp_active(const vr_context* c) {
     const vr_options& o = c->opts;
     return o.mUseLearnedPHat && !o.mUseReference && (o.mEnableTemporalReuse || o.mEnableSpatialReuse);
@@ -562,6 +572,9 @@ static bool options_valid(const vr_options* o, std::string& why) {
     for (uint32_t m : methods) if (m > VR_TRACK_ANALOG_RESIDUAL_RATIO) { why = "unknown tracking method"; return false; }
     if (o->mTemporalReprojectionMode > VR_REPROJ_NO_BACKGROUND) { why = "unknown reprojection mode"; return false; }
     if (o->mUsePrevVolumeForReproj != 0 && o->mUsePrevVolumeForReproj != 1) { why = "mUsePrevVolumeForReproj must be 0 or 1"; return false; }
+    if (o->mVertexReuse != 0 && o->mVertexReuse != 1) { why = "mVertexReuse must be 0 or 1"; return false; }
+    if (o->mVertexReuseStartBounce < 1 || o->mVertexReuseStartBounce > 64) { why = "mVertexReuseStartBounce must be in [1, 64]"; return false; }
+    if (o->mVertexReuse && o->mUseLearnedPHat) { why = "mVertexReuse is not available with mUseLearnedPHat"; return false; }
     if (o->mUseLearnedPHat) {
         if (!o->mEnableTemporalReuse && !o->mEnableSpatialReuse) { why = "mUseLearnedPHat needs temporal or spatial reuse"; return false; }
         if (o->mLearnedTrainSamples < 0 || o->mLearnedTrainSamples > (1 << 26)) { why = "mLearnedTrainSamples must be in [0, 2^26]"; return false; }
@@ -669,6 +682,8 @@ void vr_options_default(vr_options* o) {
     o->mLearnedTargetMethod = VR_TRACK_RAY_MARCHING;
     o->mLearnedLoss = 0;
     o->mUsePrevVolumeForReproj = 1;
+    o->mVertexReuse = 0;
+    o->mVertexReuseStartBounce = 1;
 }
 
 // ---- volumes ----
@@ -1191,6 +1206,8 @@ static void fill_sampling(vrd::SamplingOptions& s, uint32_t vm, uint32_t lm, int
     s.visibilityUseLinearSampler = vlin; s.lightingUseLinearSampler = llin;
     s.visibilityTStepScale = vts; s.lightingTStepScale = lts;
     s.useEnvironmentLights = o.mUseEnvironmentLights; s.useAnalyticLights = o.mUseAnalyticLights;
+    // the VERTEX_REUSE define applies to paths with indirect vertices (VolumetricReSTIR.cpp:376-386)
+    s.vertexReuseStartBounce = (o.mVertexReuse && o.mMaxBounces > 1) ? o.mVertexReuseStartBounce : -1;
 }
 
 static vrd::FrameParams frame_params(vr_context* c, const CamFrame& cam, int numTotalRounds) {
@@ -1285,6 +1302,11 @@ int vr_render_frame(vr_context* c, const vr_camera* cam, float* out_rgba, float*
     B.sp[0] = c->res[0];
     B.sp[1] = c->res[1];
     B.hist = c->res[2];
+    if (vertex_reuse(c)) {
+        B.cur.pp = B.sp[0].pp = c->ppPlane[0];
+        B.sp[1].pp = c->ppPlane[1];
+        B.hist.pp = c->ppPlane[2];
+    }
     B.featCur = c->feat[c->featCurIdx];
     B.featPrev = c->feat[c->featCurIdx ^ 1];
     B.color = o.mUseReference ? c->color : nullptr;
@@ -1432,7 +1454,7 @@ int vr_render_reference(vr_context* c, const vr_camera* cam, int32_t first_frame
 }
 
 // ---- exports ----
-int32_t vr_reservoir_bytes(const vr_context* c) { return c ? (c->opts.mMaxBounces > 1 ? 36 : 32) : 0; }
+int32_t vr_reservoir_bytes(const vr_context* c) { return c ? (c->opts.mMaxBounces > 1 ? (vertex_reuse(c) ? 40 : 36) : 32) : 0; }
 
 int vr_export_reservoirs(vr_context* c, int32_t which, void* host, size_t bytes) {
     if (!c || !host || which < 0 || which > 3) return VR_ERR_INVALID_ARG;
@@ -1446,6 +1468,11 @@ int vr_export_reservoirs(vr_context* c, int32_t which, void* host, size_t bytes)
     cudaDeviceSynchronize();
     cudaMemcpy(a.data(), c->res[idx].a, N * 16, cudaMemcpyDeviceToHost);
     cudaMemcpy(b.data(), c->res[idx].b, N * 16, cudaMemcpyDeviceToHost);
+    std::vector<float> pp;
+    if (vertex_reuse(c)) {
+        pp.resize(N);
+        cudaMemcpy(pp.data(), c->ppPlane[idx], N * 4, cudaMemcpyDeviceToHost);
+    }
     int mb = c->opts.mMaxBounces;
     char* o = (char*)host;
     for (size_t i = 0; i < N; ++i) {
@@ -1454,6 +1481,7 @@ int vr_export_reservoirs(vr_context* c, int32_t which, void* host, size_t bytes)
         memcpy(&r.lightUV[0], &b[i].x, 4); memcpy(&r.lightUV[1], &b[i].y, 4);
         r.lightID = b[i].z; r.sampledPixel = b[i].w;
         r.extraBounceStartId = (int32_t)(i * (size_t)(mb - 1));
+        r.p_partial = pp.empty() ? 0.f : pp[i];
         memcpy(o + i * rb, &r, rb);
     }
     return check_cuda(c, "export");
@@ -1924,7 +1952,7 @@ extern "C" int64_t vr_state_bytes(const vr_context* c) {
     if (!c) return 0;
     int64_t N = (int64_t)c->W * c->H;
     int64_t ne = N * std::max(c->opts.mMaxBounces - 1, 1);
-    return (int64_t)sizeof(StateHeader) + 3 * (N * 32 + ne * 16) + 2 * N * 4 + N * 16;
+    return (int64_t)sizeof(StateHeader) + 3 * (N * 32 + ne * 16) + 2 * N * 4 + N * 16 + (vertex_reuse(c) ? 3 * N * 4 : 0);
 }
 extern "C" int vr_export_state(vr_context* c, void* host, size_t bytes) {
     if (!c || !host || (int64_t)bytes < vr_state_bytes(c)) return VR_ERR_INVALID_ARG;
@@ -1942,7 +1970,9 @@ extern "C" int vr_export_state(vr_context* c, void* host, size_t bytes) {
         cudaMemcpy(p, c->res[i].extra, ne * 16, cudaMemcpyDeviceToHost); p += ne * 16;
     }
     for (int i = 0; i < 2; ++i) { cudaMemcpy(p, c->feat[i], N * 4, cudaMemcpyDeviceToHost); p += N * 4; }
-    cudaMemcpy(p, c->color, N * 16, cudaMemcpyDeviceToHost);
+    cudaMemcpy(p, c->color, N * 16, cudaMemcpyDeviceToHost); p += N * 16;
+    if (vertex_reuse(c))
+        for (int i = 0; i < 3; ++i) { cudaMemcpy(p, c->ppPlane[i], N * 4, cudaMemcpyDeviceToHost); p += N * 4; }
     return check_cuda(c, "export state");
 }
 extern "C" int vr_import_state(vr_context* c, const void* host, size_t bytes) {
@@ -1964,7 +1994,9 @@ extern "C" int vr_import_state(vr_context* c, const void* host, size_t bytes) {
         cudaMemcpy(c->res[i].extra, p, ne * 16, cudaMemcpyHostToDevice); p += ne * 16;
     }
     for (int i = 0; i < 2; ++i) { cudaMemcpy(c->feat[i], p, N * 4, cudaMemcpyHostToDevice); p += N * 4; }
-    cudaMemcpy(c->color, p, N * 16, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->color, p, N * 16, cudaMemcpyHostToDevice); p += N * 16;
+    if (vertex_reuse(c))
+        for (int i = 0; i < 3; ++i) { cudaMemcpy(c->ppPlane[i], p, N * 4, cudaMemcpyHostToDevice); p += N * 4; }
     c->frameCount = h.frameCount;
     c->temporalSampleAccumulated = h.temporalSampleAccumulated;
     c->featCurIdx = h.featCurIdx;
@@ -1989,6 +2021,7 @@ int noalloc_prepare(vr_context* c, const vr_camera* cam, int32_t frame_index, No
         return VR_ERR_INVALID_ARG;
     }
     if (o.mMaxBounces > kNoAllocMaxBounces) { c->err = "vr_render_frame_noalloc supports mMaxBounces <= 2"; return VR_ERR_INVALID_ARG; }
+    if (vertex_reuse(c)) { c->err = "vr_render_frame_noalloc does not keep p_partial: disable mVertexReuse"; return VR_ERR_INVALID_ARG; }
     if (lp_active(c)) {
         // the learned target needs its vertex records, queries and network buffers, which this
         // entry point has no room for: refuse rather than render the plain form silently
@@ -2359,6 +2392,7 @@ int vr_set_block_size(vr_context* c, int32_t threads) {
 int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
     if (!ctxs || !out || n < 1 || n > 1024) return VR_ERR_INVALID_ARG;
     for (int i = 0; i < n; ++i) if (!ctxs[i] || !ctxs[i]->anim.empty()) return VR_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i) if (vertex_reuse(ctxs[i])) return VR_ERR_UNSUPPORTED;    // batches keep no p_partial
     const vr_options& o0 = ctxs[0]->opts;
     if (o0.mUseReference) return VR_ERR_INVALID_ARG;
     for (int i = 1; i < n; ++i) {

@@ -103,6 +103,7 @@ struct SamplingOptions {         // HostDeviceSharedDefinitions.h:96-141
     int visibilityUseLinearSampler, lightingUseLinearSampler;
     float visibilityTStepScale, lightingTStepScale;
     int useEnvironmentLights, useAnalyticLights;
+    int vertexReuseStartBounce;  // vertex reuse (VERTEX_REUSE): the first reconnection bounce; -1 off
 };
 
 struct FrameParams {
@@ -130,6 +131,7 @@ struct ResBuf {
     float4* a;
     int4* b;
     float4* extra;
+    float* pp;             // p_partial per pixel under vertex reuse, else nullptr
 };
 
 // Each translation unit that includes this header has its own copy of the scene constants
@@ -152,11 +154,12 @@ struct Reservoir {
     float uv0, uv1;
     int lightID, sampledPixel;
     int startPixel;              // extraBounceStartId / (maxBounces - 1)
+    float pp;                    // p_partial (vertex reuse): the suffix's share of p_hat
 };
 __device__ __forceinline__ Reservoir newReservoir() {
     Reservoir r;
     r.runningSum = 0.f; r.M = 0.f; r.depth = kRayTMax; r.p_y = 0.f;
-    r.uv0 = 0.f; r.uv1 = 0.f; r.lightID = 0; r.sampledPixel = 0; r.startPixel = 0;
+    r.uv0 = 0.f; r.uv1 = 0.f; r.lightID = 0; r.sampledPixel = 0; r.startPixel = 0; r.pp = 0.f;
     return r;
 }
 __device__ __forceinline__ Reservoir loadRes(const ResBuf& buf, int i) {
@@ -166,6 +169,7 @@ __device__ __forceinline__ Reservoir loadRes(const ResBuf& buf, int i) {
     r.runningSum = a.x; r.M = a.y; r.depth = a.z; r.p_y = a.w;
     r.uv0 = __int_as_float(b.x); r.uv1 = __int_as_float(b.y); r.lightID = b.z; r.sampledPixel = b.w;
     r.startPixel = i;
+    r.pp = buf.pp ? __ldg(&buf.pp[i]) : 0.f;
     return r;
 }
 // coherent load (buffer written earlier in the same kernel)
@@ -176,15 +180,18 @@ __device__ __forceinline__ Reservoir loadResRW(const ResBuf& buf, int i) {
     r.runningSum = a.x; r.M = a.y; r.depth = a.z; r.p_y = a.w;
     r.uv0 = __int_as_float(b.x); r.uv1 = __int_as_float(b.y); r.lightID = b.z; r.sampledPixel = b.w;
     r.startPixel = i;
+    r.pp = buf.pp ? buf.pp[i] : 0.f;
     return r;
 }
 __device__ __forceinline__ void storeRes(const ResBuf& buf, int i, const Reservoir& r) {
     buf.a[i] = make_float4(r.runningSum, r.M, r.depth, r.p_y);
     buf.b[i] = make_int4(__float_as_int(r.uv0), __float_as_int(r.uv1), r.lightID, r.sampledPixel);
+    if (buf.pp) buf.pp[i] = r.pp;
 }
 __device__ __forceinline__ void copySample(const Reservoir& f, Reservoir& t) {
     t.depth = f.depth; t.p_y = f.p_y; t.uv0 = f.uv0; t.uv1 = f.uv1;
     t.lightID = f.lightID; t.startPixel = f.startPixel; t.sampledPixel = f.sampledPixel;
+    t.pp = f.pp;                 // Reservoir.slang:46-48, 76-78
 }
 __device__ __forceinline__ bool resampleStep(const Reservoir& r, Reservoir& s, vr::Rng& sg) {
     float w = r.runningSum;
@@ -1213,9 +1220,11 @@ struct DirectVis {
         return computeVisibility(r, sg, samples, mip, lin, method, tss);
     }
 };
+// pre / reuse: vertex reuse takes the light transmittance from the reservoir's p_partial, or hands
+// the estimated one back for it (ReSTIRHelper.slang:443-496)
 template <class V>
 __device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, float uv0, float uv1, vr::Rng& sg, const SamplingOptions& o, bool cull,
-                                       int off, V& vis) {
+                                       int off, V& vis, float* pre = nullptr, bool reuse = false) {
     Ray sr;
     f3 Ld;
     if (lid < 0) {
@@ -1230,16 +1239,29 @@ __device__ inline f3 evalLightInVolume(const MediumInteraction& mi, int lid, flo
     } else {
         return mk3(0.f);
     }
-    float Tr = vis(sr, sg, o.lightSamples, cull ? o.lightingMipLevel + off : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
+    float Tr;
+    if (reuse) Tr = *pre;
+    else {
+        Tr = vis(sr, sg, o.lightSamples, cull ? o.lightingMipLevel + off : 0, o.lightingUseLinearSampler != 0, o.lightingTrackingMethod, o.lightingTStepScale);
+        if (pre) *pre = Tr;
+    }
     return Tr * Ld;
 }
 
 // extra: the extra-bounce plane base, indexed extra[b * N + tap.startPixel]; lastFrame: the
 // sample as of the previous frame (the temporal tap's MIS weight), on the previous animation
 // frame's grids when the volume is animated and usePrevGrid is set
+// spatialReuse / ppOut: vertex reuse (the reservoir is REUSETYPE inout in ReSTIRHelper.slang:91-420):
+// spatial reuse takes the suffix's share of p_hat from tap.pp; other calls write the share they
+// evaluate to *ppOut (when given)
 template <class V>
 static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4* extra, int N, Ray ray, vr::Rng& sg, const SamplingOptions& o,
-                                             int maxBounces, bool noReuse, bool isFinal, bool lastFrame, V& vis) {
+                                             int maxBounces, bool noReuse, bool isFinal, bool lastFrame, V& vis, bool spatialReuse = false,
+                                             float* ppOut = nullptr) {
+    const int vrs = o.vertexReuseStartBounce;
+    const bool vreuse = vrs >= 0;
+    f3 P_prefix = mk3(1.f);
+    int bounceId = 0;
     const bool useLast = lastFrame && c_scene.usePrevGrid && c_scene.hasAnimation;
     const int off = useLast ? kPrevSlotOffset : 0;
     bool isBg = tap.depth == kRayTMax;
@@ -1269,16 +1291,24 @@ static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4*
             Ray sr{};
             if (maxBounces > 1 && mib > 0) {
                 scatterEm = decodeTag(tap.sampledPixel) == 1;
-                for (int b = 0; b < mib; b++) {
+                for (; bounceId < mib; bounceId++) {
+                    const int b = bounceId;
                     bool curEm = scatterEm && b == mib - 1;
                     float4 e = extra[(size_t)b * N + tap.startPixel];
-                    // decodeWiDist (ReSTIRHelper.slang:21-39), direction form
-                    f3 wi = mk3(e.x, e.y, vr::sqrt_(1.0f - (e.x * e.x + e.y * e.y)));
-                    if (vr::isnan_(wi.z)) wi.z = 0.f;
-                    float wz = e.z;
-                    if (wz < 0) { wi.z = -wi.z; wz = -wz; }
-                    float wx = wi.x, wy = wi.y, wzz = wi.z, ww = wz;
-                    if (curEm) { wx = tap.uv0; wy = tap.uv1; wzz = __int_as_float(tap.lightID); ww = -1.f; }
+                    float wx, wy, wzz, ww;
+                    if (vreuse && b + 1 >= vrs) {
+                        // decodeWiDist (ReSTIRHelper.slang:21-39), vertex form (vertex reuse)
+                        if (e.x == kRayTMax) { wx = 0.f; wy = 0.f; wzz = 0.f; ww = kRayTMax; }
+                        else { wx = e.x; wy = e.y; wzz = e.z; ww = -1.f; }
+                    } else {
+                        // decodeWiDist, direction form
+                        f3 wi = mk3(e.x, e.y, vr::sqrt_(1.0f - (e.x * e.x + e.y * e.y)));
+                        if (vr::isnan_(wi.z)) wi.z = 0.f;
+                        float wz = e.z;
+                        if (wz < 0) { wi.z = -wi.z; wz = -wz; }
+                        wx = wi.x; wy = wi.y; wzz = wi.z; ww = wz;
+                    }
+                    if (curEm && (!vreuse || b + 1 < vrs)) { wx = tap.uv0; wy = tap.uv1; wzz = __int_as_float(tap.lightID); ww = -1.f; }
                     if (ww == kRayTMax) return mk3(0.f);
                     float dist = 1.f;
                     if (ww == -1.f) {
@@ -1290,6 +1320,10 @@ static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4*
                     }
                     F = F * mk3(phaseF(mi, mi.wo, sr.d));
                     if (vr::all_eq0(F)) return mk3(0.f);
+                    if (vreuse && b == vrs) {                // ReSTIRHelper.slang:289-295
+                        if (spatialReuse) return F * tap.pp;
+                        P_prefix = F;
+                    }
                     pW = ww == -1.f ? mk3(wx, wy, wzz) : at(sr, sr.tMax);
                     f3 sig; float sd;
                     if (!noReuse) {
@@ -1300,7 +1334,7 @@ static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4*
                         sd = 1.f;
                     }
                     F = F * (sd * sig);
-                    if (curEm) F = F * (1.f / (dist * dist));
+                    if (vreuse ? (b + 1 == vrs || (curEm && b + 1 < vrs)) : curEm) F = F * (1.f / (dist * dist));
                     if (vr::all_eq0(F)) return mk3(0.f);
                     float sv = 1.f;
                     if (!noReuse)
@@ -1313,10 +1347,17 @@ static __device__ __noinline__ f3 evaluateFV(const Reservoir& tap, const float4*
                 if (scatterEm) F = F * emissionWorld(pW, useLast);
                 else mi = MediumInteraction{at(sr, sr.tMax), -sr.d, c_scene.g, true};
             }
-            if (!scatterEm && vr::any_gt0(F))
-                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal, off, vis);
+            if (!scatterEm && vr::any_gt0(F)) {
+                const bool reuse = vreuse && bounceId == vrs && spatialReuse;
+                float pre = tap.pp;
+                F = F * evalLightInVolume(mi, tap.lightID, tap.uv0, tap.uv1, sg, o, !isFinal, off, vis, &pre, reuse);
+                if (vreuse && bounceId == vrs && !spatialReuse && ppOut) *ppOut = pre;
+            }
         }
     }
+    // ReSTIRHelper.slang:415-419: the suffix's share of p_hat
+    if (vreuse && bounceId > vrs && !spatialReuse && ppOut)
+        *ppOut = vr::luminance(mk3(F.x / P_prefix.x, F.y / P_prefix.y, F.z / P_prefix.z));
     return F;
 }
 __device__ __forceinline__ f3 evaluateF(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o,
@@ -1324,13 +1365,18 @@ __device__ __forceinline__ f3 evaluateF(const Reservoir& tap, const float4* extr
     DirectVis v;
     return evaluateFV<DirectVis>(tap, extra, N, ray, sg, o, maxBounces, noReuse, isFinal, lastFrame, v);
 }
+// spatialReuse / ppOut as in evaluateFV (vertex reuse)
 __device__ __forceinline__ float evalPHat(const Reservoir& tap, const float4* extra, int N, const Ray& ray, vr::Rng& sg, const SamplingOptions& o, int mb,
-                                         bool lastFrame = false) {
-    return vr::luminance(evaluateF(tap, extra, N, ray, sg, o, mb, false, false, lastFrame));
+                                         bool lastFrame = false, bool spatialReuse = false, float* ppOut = nullptr) {
+    DirectVis v;
+    return vr::luminance(evaluateFV<DirectVis>(tap, extra, N, ray, sg, o, mb, false, false, lastFrame, v, spatialReuse, ppOut));
 }
-__device__ __forceinline__ void resampleNeighbor(Reservoir& tap, const Ray& ray, vr::Rng& sg, const float4* extra, int N, const SamplingOptions& o, int mb) {
+// resampleNeighbor (the tap's p_partial re-evaluated: REUSETYPE inout) and, with spatialReuse,
+// resampleNeighborSpatialReuse (ReSTIRHelper.slang:567-600)
+__device__ __forceinline__ void resampleNeighbor(Reservoir& tap, const Ray& ray, vr::Rng& sg, const float4* extra, int N, const SamplingOptions& o, int mb,
+                                                 bool spatialReuse = false) {
     if (tap.runningSum == 0.f) return;
-    float ph = evalPHat(tap, extra, N, ray, sg, o, mb);
+    float ph = evalPHat(tap, extra, N, ray, sg, o, mb, false, spatialReuse, spatialReuse ? nullptr : &tap.pp);
     float w = ph / tap.p_y;
     if (vr::isinf_(w) || vr::isnan_(w)) w = 0.f;
     tap.runningSum *= w;

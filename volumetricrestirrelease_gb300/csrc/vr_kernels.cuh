@@ -64,6 +64,12 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
             mi.p = at(ray, hitD); mi.wo = -ray.d; mi.g = c_scene.g; mi.valid = hitD != kRayTMax;
         }
         pathPdf *= pdfDist;
+        const int vrs = o.vertexReuseStartBounce;
+        // ComputeInitialSample.slang:88-94: the reconnection vertex in area measure (vertex reuse)
+        if (vrs >= 0 && bounce == vrs && hitD != kRayTMax) {
+            pathPdf /= hitD * hitD;
+            pathPHat /= hitD * hitD;
+        }
         bool hitEmpty = false;
         float density = 0.f;
         if (bounce == 0) {
@@ -75,10 +81,15 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
             out.depth = primaryDepth;
             if (MB > 1) {
                 out.sampledPixel = encodeBounces(out.sampledPixel, bounce);
-                // encodeWiDist (ReSTIRHelper.slang:41-51)
-                f3 w = mk3(ray.d.x, ray.d.y, !mi.valid ? kRayTMax : hitD);
-                if (ray.d.z < 0) w.z = -w.z;
-                ex[bounce - 1] = w;
+                if (vrs >= 0 && bounce >= vrs) {
+                    // vertex reuse: from the reuse bounce on, the vertex position (ComputeInitialSample.slang:114-127)
+                    ex[bounce - 1] = !mi.valid ? mk3(kRayTMax) : mi.p;
+                } else {
+                    // encodeWiDist (ReSTIRHelper.slang:41-51)
+                    f3 w = mk3(ray.d.x, ray.d.y, !mi.valid ? kRayTMax : hitD);
+                    if (ray.d.z < 0) w.z = -w.z;
+                    ex[bounce - 1] = w;
+                }
             }
             out.p_y = pathPdf;
         }
@@ -127,8 +138,10 @@ static __device__ __noinline__ Reservoir initialSample(const FrameParams& P, Ray
                     if (out.runningSum > 0.f) {
                         out.runningSum = out.p_y == 0.f ? 0.f : p_y / out.p_y;
                         if (out.lightID == kSelfEmissionLightID && bounce > 0) {
-                            out.lightID = vr::asint(mi.p.z); out.uv0 = mi.p.x; out.uv1 = mi.p.y;
-                            p_y /= (hitD * hitD);
+                            if (vrs < 0 || bounce < vrs) {       // ComputeInitialSample.slang:322-330
+                                out.lightID = vr::asint(mi.p.z); out.uv0 = mi.p.x; out.uv1 = mi.p.y;
+                                p_y /= (hitD * hitD);
+                            }
                             out.sampledPixel = encodeTag(out.sampledPixel, 1);
                         }
                         out.p_y = p_y;
@@ -384,7 +397,8 @@ __device__ __forceinline__ void initialPixel(const FrameParams& P, const FrameBu
     const int mib0 = decodeBounces(fin.sampledPixel, MB);
     for (int b = 0; b < mib0; b++) B.cur.extra[(size_t)b * N + pid] = make_float4(finalEx[b].x, finalEx[b].y, finalEx[b].z, 0.f);
     fin.startPixel = pid;
-    float ph = evalPHat(fin, B.cur.extra, N, ray, sg, P.spatial, MB);
+    // TraceRays.cs.slang:176-177 (the reservoir is REUSETYPE inout: vertex reuse updates p_partial)
+    float ph = evalPHat(fin, B.cur.extra, N, ray, sg, P.spatial, MB, false, false, &fin.pp);
     if (fin.runningSum > 0.f) {
         fin.runningSum *= fin.p_y == 0.f ? 0.f : ph / fin.p_y;
         fin.p_y = ph;
@@ -478,7 +492,7 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
             if (!(tx >= 0 && tx < W && ty >= 0 && ty < H)) continue;
             Reservoir tap = loadRes(in, ty * W + tx);
             float mis = 1.f;
-            if (s > 0) resampleNeighbor(tap, ray, sg, in.extra, N, P.spatial, MB);
+            if (s > 0) resampleNeighbor(tap, ray, sg, in.extra, N, P.spatial, MB, true);     // resampleNeighborSpatialReuse
             if (P.spatialTalbot && tap.runningSum > 0.f) {
                 float p_sum = 0, p_qi = 0, k = 0;
                 for (int j = 0; j < K; j++) {
@@ -491,7 +505,7 @@ __device__ __forceinline__ void spatialPixel(const FrameParams& P, const FrameBu
                     else if (s == j) { p_qi = a2.w; p_sum += a2.w * M2; }
                     else {
                         Ray nr{ray.o, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, tx2, ty2, W, H)), 0, tap.depth};
-                        float p_y = evalPHat(tap, in.extra, N, nr, sg, P.spatial, MB);
+                        float p_y = evalPHat(tap, in.extra, N, nr, sg, P.spatial, MB, false, true);    // evaluatePHatReadOnly(..., true)
                         if (vr::isinf_(p_y) || vr::isnan_(p_y)) p_y = 0.f;
                         p_sum += p_y * M2;
                     }
@@ -591,7 +605,7 @@ struct ReplayVis {
     }
 };
 __host__ __device__ inline bool spatialSplitEligible(const FrameParams& P) {
-    return P.spatialK <= kSplitK && P.spatial.visibilityTrackingMethod == VR_TRACK_RAY_MARCHING &&
+    return P.spatial.vertexReuseStartBounce < 0 && P.spatialK <= kSplitK && P.spatial.visibilityTrackingMethod == VR_TRACK_RAY_MARCHING &&
            P.spatial.lightingTrackingMethod == VR_TRACK_RAY_MARCHING && P.spatial.visibilitySamples == 1 && P.spatial.lightSamples == 1;
 }
 

@@ -452,9 +452,14 @@ class Accumulator:
 RESERVOIR_DTYPE_36 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
                                ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4"),
                                ("extraBounceStartId", "<i4")])
+RESERVOIR_DTYPE_40 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
+                               ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4"),
+                               ("extraBounceStartId", "<i4"), ("p_partial", "<f4")])
 RESERVOIR_DTYPE_32 = np.dtype([("runningSum", "<f4"), ("M", "<f4"), ("depth", "<f4"), ("p_y", "<f4"),
                                ("lightUV", "<f4", 2), ("lightID", "<i4"), ("sampledPixel", "<i4")])
 
 
-def as_reservoirs(buf, max_bounces):
+def as_reservoirs(buf, max_bounces, vertex_reuse=False):
+    if max_bounces > 1 and vertex_reuse:
+        return np.frombuffer(buf.tobytes(), RESERVOIR_DTYPE_40)
     return np.frombuffer(buf.tobytes(), RESERVOIR_DTYPE_36 if max_bounces > 1 else RESERVOIR_DTYPE_32)
