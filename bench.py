@@ -6,14 +6,17 @@ lights + procedural sky, camera orbiting 0.5 deg per frame.  Synthetic data (the
 clouds are not available).
 
 Metric: 1080p frames/s of the learned-target form (transmittance MLP in the initial RIS target,
-FP16 bricks) with LEARNED_M candidates, the count at which its relMSE against the FP64
-path-traced reference matches the plain form's (FP32 bricks, 32 candidates).  The match is
-checked in the run: both forms render the orbiting camera path at 960x540 for 128 frames, and
-at every 8th frame from 32 on each image's relMSE is taken against a 512-spp FP64 reference of
-that frame rendered on the GPU.  The learned form at candidate count M matches when the mean of
-the per-frame differences (learned - plain) is at most one standard error of that mean above
-zero; the sweep over several M also gives the count at equal relMSE by interpolation.  The plain
-form's frames/s is reported beside the learned form's.
+FP16 bricks, LEARNED_M candidates) against the plain form (FP32 bricks) at matched relMSE.  The
+match is made in the run: every form renders the orbiting camera path at 960x540 for 128
+frames, and at every 8th frame from 32 on each image's relMSE is taken against a 512-spp FP64
+reference of that frame rendered on the GPU.  The plain form runs at several candidate counts
+(PLAIN_SWEEP_M and 32); the count at which its relMSE equals the learned form's is interpolated
+linearly in 1/M between the two sweep counts that bracket it, and the plain form's 1080p
+frame time at that count linearly in M between its timed frames at those two counts.  The
+speed-up at equal relMSE is the learned form's frames/s over that plain frames/s.  Beside it:
+the paired per-frame comparison of the learned form with the plain form at 32 candidates (mean
+difference, standard error, z) and with the two bracketing plain counts, and a learned-form
+sweep over SWEEP_M.
 
 Output: one JSON line (rank 0).  `value` = frames/s with every input resident in HBM
 (vr_render_frame into a device buffer, CUDA events on the launching stream); `e2e` = the same
@@ -50,11 +53,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "1080p frames/s at matched relMSE vs FP64 ref; learned-p-hat vs plain, 1 GB300"
 WORKLOAD = ("learned-p-hat + FP16-brick ReSTIR frame, 1920x1080, 512^3 sparse fBm (8^3 bricks, 4-level conservative mips), "
             "max path length 3, temporal + 3 spatial neighbours, 16 point lights + 512x256 sky, orbiting camera; "
-            "candidate count matched to the plain form's relMSE (plain: FP32 bricks, M=32)")
-# the learned form's candidate count: the quality sweep (960x540, orbiting camera) finds its
-# relMSE not above the plain form's (32 candidates) by more than one standard error at this count
+            "36 candidates; the plain form (FP32 bricks) compared at the candidate count of equal relMSE")
+# the learned form's candidate count (fixed; the learned sweep below shows how its relMSE moves
+# with the count), the plain form's counts for the equal-relMSE interpolation (with 32), and the
+# learned form's sweep
 LEARNED_M = 36
-SWEEP_M = (28, 32, 36, 40, 48)
+PLAIN_SWEEP_M = (8, 12, 16, 24)
+SWEEP_M = (24, 36, 48)
 
 
 def _peaks():
@@ -241,28 +246,35 @@ def quality(lib, vols, args, forms, QW=960, QH=540, frames=128, first=32, every=
     return res, info
 
 
-def match_candidates(rel, sweep):
-    """The paired comparison of each learned count with the plain form: mean per-frame relMSE
-    difference, its standard error, z = mean / SE, and the count at equal relMSE interpolated
-    linearly in 1/M between the sweep's neighbours."""
-    p = rel["plain"]
-    out = {}
-    for M in sweep:
-        d = rel[f"learned_M{M}"] - p
-        se = float(d.std(ddof=1) / np.sqrt(len(d))) if len(d) > 1 else float("inf")
-        out[M] = {"relmse": float(rel[f"learned_M{M}"].mean()), "diff": float(d.mean()), "se": se,
-                  "z": float(d.mean() / se) if se > 0 else float("inf")}
-    equal = None
-    ms = sorted(sweep)
-    for a, b in zip(ms, ms[1:]):
-        da, db = out[a]["diff"], out[b]["diff"]
-        if da > 0 >= db:
-            t = da / (da - db)
-            equal = 1.0 / (1.0 / a + t * (1.0 / b - 1.0 / a))
-            break
-    if equal is None and out[ms[0]]["diff"] <= 0:
-        equal = float(ms[0])
-    return out, equal
+def paired(rel, a, b):
+    """The paired comparison of forms a and b over the evaluated frames: mean per-frame relMSE
+    difference (a - b), its standard error and z = mean / SE."""
+    d = rel[a] - rel[b]
+    se = float(d.std(ddof=1) / np.sqrt(len(d))) if len(d) > 1 else float("inf")
+    return {"relmse": float(rel[a].mean()), "diff": float(d.mean()), "se": se, "z": float(d.mean() / se) if se > 0 else float("inf")}
+
+
+def plain_key(M):
+    return "plain" if M == 32 else f"plain_M{M}"
+
+
+def equal_relmse(rel, learned_key, plain_ms):
+    """The plain form's candidate count at the learned form's relMSE, interpolated linearly in 1/M
+    between the two plain counts whose relMSE brackets it, and the plain form's 1080p frame time
+    there, interpolated linearly in M between its timed frames at those counts.  plain_ms: {M:
+    ms per frame}.  None when the learned relMSE lies outside the plain sweep."""
+    target = float(rel[learned_key].mean())
+    ms = sorted(plain_ms)
+    r = {M: float(rel[plain_key(M)].mean()) for M in ms}
+    for lo, hi in zip(ms, ms[1:]):
+        if r[lo] >= target >= r[hi] and r[lo] > r[hi]:
+            t = (r[lo] - target) / (r[lo] - r[hi])
+            m_eq = 1.0 / (1.0 / lo + t * (1.0 / hi - 1.0 / lo))
+            frame_ms = plain_ms[lo] + (m_eq - lo) / (hi - lo) * (plain_ms[hi] - plain_ms[lo])
+            return {"candidates": m_eq, "bracket": [lo, hi], "plain_relmse": [r[lo], r[hi]], "learned_relmse": target,
+                    "plain_ms_per_frame": frame_ms, "plain_frames_per_s": 1000.0 / frame_ms,
+                    "vs_bracket": {str(lo): paired(rel, learned_key, plain_key(lo)), str(hi): paired(rel, learned_key, plain_key(hi))}}
+    return None
 
 
 def _time_frames(rd, sc, out, sptr, warmup, steps, first=0, clock_index=None, barrier=lambda: None):
@@ -459,25 +471,27 @@ def run_batched(args, lib):
     # the same instances rendered one after another, each by its own vr_render_frame (the
     # alternative to batching)
     fs = f + args.batch_steps
-    for k in range(2):
+    ms_seq = None
+    for k in (range(2) if not args.no_batch_sequential else ()):
         for r, sc, o in zip(rends, descs, ptrs):
             r.execute(sc.camera(fs + k), o)
-    torch.cuda.synchronize()
-    e0.record()
-    for k in range(2, 2 + args.batch_steps):
-        for r, sc, o in zip(rends, descs, ptrs):
-            r.execute(sc.camera(fs + k), o)
-    e1.record()
-    torch.cuda.synchronize()
-    ms_seq = e0.elapsed_time(e1) / args.batch_steps
+    if not args.no_batch_sequential:
+        torch.cuda.synchronize()
+        e0.record()
+        for k in range(2, 2 + args.batch_steps):
+            for r, sc, o in zip(rends, descs, ptrs):
+                r.execute(sc.camera(fs + k), o)
+        e1.record()
+        torch.cuda.synchronize()
+        ms_seq = e0.elapsed_time(e1) / args.batch_steps
     res = {"workload": "32 instances (8 fire plumes), resolutions from {256^2, 512^2, 960x540, 1280x720, 1920x1080}, "
                        "128^3..512^3 sparse fBm, max path length 3, 16..32 candidates, temporal + spatial, FP16 bricks, "
                        "learned target (2^15 training samples per instance and frame)",
            "instances": len(descs), "pixels_per_frame": px, "ms_per_batch_frame": ms, "batch_frames_per_s": 1000.0 / ms,
            "pixels_per_s": px * 1000.0 / ms, "equivalent_1080p_frames_per_s": px * 1000.0 / ms / (1920 * 1080),
-           "sequential": {"ms_per_frame": ms_seq, "pixels_per_s": px * 1000.0 / ms_seq,
+           "sequential": {"ms_per_frame": ms_seq, "pixels_per_s": px * 1000.0 / ms_seq if ms_seq else None,
                           "what": "the 32 instances rendered one after another with vr_render_frame"},
-           "speedup_vs_sequential": ms_seq / ms,
+           "speedup_vs_sequential": ms_seq / ms if ms_seq else None,
            "graph": True, "launches_per_frame": launches,
            "autotune": {"chosen_tile": f"{shape[0]}x{shape[1]}", "blocks_per_sm": shape[2], "trial_ms": trials,
                         "candidates": "tiles 8x16, 16x8, 32x4 x 5, 3, 8 blocks per SM (first trials)"},
@@ -637,6 +651,10 @@ def run_gpu(args):
     W, H = args.width, args.height
     t0 = time.time()
     vols = {False: Volume.procedural(_scene(args).volume, lib=lib), True: Volume.procedural(_scene(args, fp16=True).volume, lib=lib)}
+    if args.only_batched:
+        # the batched form alone (profiling runs)
+        print(json.dumps({"batched": run_batched(args, lib)}), flush=True)
+        return
     vols["bc4"] = Volume.procedural(_scene(args).volume, lib=lib).compress_bc4()
     build_s = time.time() - t0
 
@@ -646,12 +664,15 @@ def run_gpu(args):
 
     # ---- relMSE matching (960x540, the orbiting camera path, per-frame FP64 references) ----
     forms = {"plain": (False, False, 32), "plain_fp16": (True, False, 32), "plain_bc4": (False, False, 32, "bc4")}
+    for M in PLAIN_SWEEP_M:
+        forms[plain_key(M)] = (False, False, M)
     for M in SWEEP_M:
         forms[f"learned_M{M}"] = (True, True, M)
     rel, qinfo = quality(lib, vols, args, forms) if not args.no_quality else ({}, {})
-    match, m_equal = match_candidates(rel, SWEEP_M) if rel else ({}, None)
     M_sel = LEARNED_M
-    matched = bool(match) and match[M_sel]["z"] <= 1.0
+    lkey = f"learned_M{M_sel}"
+    sweep = {str(M): paired(rel, f"learned_M{M}", "plain") for M in SWEEP_M} if rel else {}
+    vs32 = sweep.get(str(M_sel))
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     out = torch.empty((H, W, 4), device="cuda", dtype=torch.float32)
@@ -701,6 +722,18 @@ def run_gpu(args):
     msp, kmsp, _, _ = _time_frames(rp, scp, out, sptr, args.warmup, args.steps, barrier=barrier)
     plain_fps = whole_job_rate(ws, args.steps, max_over_ranks(msp, ws))
     del rp
+    # the plain form at the sweep's other counts, for the frame time at equal relMSE
+    plain_ms = {32: max_over_ranks(msp, ws) / args.steps}
+    sweep_steps = min(args.steps, 5)
+    for M in (PLAIN_SWEEP_M if rel else ()):
+        rq = VolumetricReSTIR(W, H, _options(lib, scp, False, M).as_dict(), lib=lib)
+        rq.setScene(vols[False], scp.medium, scp.lights, scp.env_rgb, scp.env_scale)
+        msq, _, _, _ = _time_frames(rq, scp, out, sptr, args.warmup, sweep_steps, barrier=barrier)
+        plain_ms[M] = max_over_ranks(msq, ws) / sweep_steps
+        del rq
+    eq = equal_relmse(rel, lkey, plain_ms) if rel else None
+    # at equal relMSE the plain form renders one replica per rank like the learned form
+    plain_eq_fps = ws * eq["plain_frames_per_s"] if eq else None
     # ---- plain form on BC4 coarse and conservative mips (the reference's texture form) ----
     rb = VolumetricReSTIR(W, H, optp.as_dict(), lib=lib)
     rb.setScene(vols["bc4"], scp.medium, scp.lights, scp.env_rgb, scp.env_scale)
@@ -760,13 +793,16 @@ def run_gpu(args):
         roof_tc = {"bound": "tensor", "kernel": "k_net_infer", "achieved": tf, "peak": pk[0], "unit": "TFLOP/s",
                    "frac": tf / pk[0] if pk[0] else None, "peak_source": pk[1], "queries_per_frame": queries,
                    "flop_per_query": NET_FLOP_PER_QUERY, "kernel_ms": kernel_ms["k_net_infer"]}
-    mt = match.get(M_sel, {})
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (bf16 MLP, fp16 bricks)", "data": "synthetic",
-            "relmse_summary": {"matched": matched, "learned": mt.get("relmse"), "plain": float(rel["plain"].mean()) if rel else None,
-                               "z": mt.get("z"), "candidates": M_sel, "equal_relmse_candidates": m_equal},
-            "plain_value": plain_fps, "speedup_learned_vs_plain": value / plain_fps,
+            "relmse_summary": {"matched": eq is not None, "learned": float(rel[lkey].mean()) if rel else None, "candidates": M_sel,
+                               "plain_candidates_at_equal_relmse": eq["candidates"] if eq else None,
+                               "plain_value_at_equal_relmse": plain_eq_fps,
+                               "speedup_at_equal_relmse": value / plain_eq_fps if eq else None,
+                               "vs_plain_m32": vs32},
+            "plain_value": plain_eq_fps, "speedup_learned_vs_plain": value / plain_eq_fps if eq else None,
+            "plain_m32_value": plain_fps, "speedup_vs_plain_m32": value / plain_fps,
             "config": _config(args, M_sel, ws),
             "e2e": {"value": e2e, "unit": "frames/s", "h2d_bytes_per_step": int(h2d.value), "d2h_bytes_per_step": int(d2h.value)},
             "gpu_launches": launches,
@@ -782,9 +818,13 @@ def run_gpu(args):
                       "bc4": {"value": bc4_fps, "unit": "frames/s", "frames": bc4_steps, "kernel_ms": {"k_initial": kmsb[0], "k_spatial": kmsb[1]},
                               "bricks": "mip 0 fp32; coarse and conservative mips BC4",
                               "relmse": float(rel["plain_bc4"].mean()) if rel else None}},
-            "relmse": {"matched": matched, "criterion": "mean per-frame relMSE difference (learned - plain) <= 1 standard error",
-                       "plain": float(rel["plain"].mean()) if rel else None,
-                       "sweep": {str(k): v for k, v in match.items()}, "equal_relmse_candidates": m_equal,
+            "relmse": {"matched": eq is not None,
+                       "criterion": ("the plain form's candidate count at the learned form's relMSE, interpolated in 1/M "
+                                     "between the bracketing plain counts; its 1080p frame time interpolated in M"),
+                       "equal_relmse": eq,
+                       "plain": {str(M): float(rel[plain_key(M)].mean()) for M in sorted(plain_ms)} if rel else None,
+                       "plain_ms_per_frame_1080p": {str(M): v for M, v in sorted(plain_ms.items())},
+                       "learned_sweep_vs_plain_m32": sweep,
                        "plain_fp16": float(rel["plain_fp16"].mean()) if rel else None, **qinfo},
             "batched": batched,
             "small_configs": small,
@@ -809,6 +849,8 @@ def main():
     ap.add_argument("--no-animated", action="store_true", help="skip the animated-volume measurement")
     ap.add_argument("--batch-steps", type=int, default=4)
     ap.add_argument("--batch-trials", type=int, default=6)
+    ap.add_argument("--only-batched", action="store_true", help="run the batched form alone and print its summary")
+    ap.add_argument("--no-batch-sequential", action="store_true", help="skip the batch's one-after-another comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else max(args.warmup, 0)
     if args.impl == "reference":
