@@ -179,7 +179,7 @@ def stream_bytes_per_pixel(mb, K):
 
 
 def generate_stream_bytes_per_pixel(M, vertices_px, queries_px):
-    """k_lp_generate's algorithmic stream bytes per pixel: feature 4 B, random state 16 B,
+    """The generate stage's algorithmic stream bytes per pixel: feature 4 B, random state 16 B,
     candidate record 8 B per candidate, vertex record 32 B per vertex, suffix record 16 B per
     indirect vertex, query 32 B + slot index 4 B per query."""
     return 4 + 16 + 8 * M + 32 * vertices_px + 16 * max(vertices_px - M, 0) + 36 * queries_px
@@ -494,7 +494,7 @@ def run_batched(args, lib):
            "speedup_vs_sequential": ms_seq / ms if ms_seq else None,
            "graph": True, "launches_per_frame": launches,
            "autotune": {"chosen_tile": f"{shape[0]}x{shape[1]}", "blocks_per_sm": shape[2], "trial_ms": trials,
-                        "candidates": "tiles 8x16, 16x8, 32x4 x 5, 3, 8 blocks per SM (first trials)"},
+                        "candidates": "tiles 8x16, 16x8, 32x4 x 5, 4, 3 blocks per SM (each pass capped at the blocks it keeps resident)"},
            "volume_build_s": round(build_s, 1), "timed_frames": args.batch_steps}
     return res
 
@@ -684,7 +684,7 @@ def run_gpu(args):
     ms, kms, launches, clocks = _time_frames(rd, sc, out, sptr, args.warmup, args.steps, clock_index=local, barrier=barrier)
     ms = max_over_ranks(ms, ws)
     value = whole_job_rate(ws, args.steps, ms)
-    stage_names = ["initial_stage", "spatial_final", "training", "k_lp_generate", "k_net_infer", "k_lp_select"]
+    stage_names = ["initial_stage", "spatial_final", "training", "generate_stage", "k_net_infer", "k_lp_select"]
     kernel_ms = dict(zip(stage_names, kms))
 
     # ---- learned form, end to end through the pipelined host entry point, on the same frames
@@ -766,22 +766,22 @@ def run_gpu(args):
                           f"median of 3 full {W}x{H} frames after 1 untimed"),
                "ms_per_frame": [1000.0 * t for t in ct]}
         lpc = roofline_counts(args, threads, M_sel, net_params, net_box)
-    dom = max(("k_lp_generate", "k_net_infer", "k_lp_select", "spatial_final", "training"), key=lambda k: kernel_ms[k] or 0.0)
+    dom = max(("generate_stage", "k_net_infer", "k_lp_select", "spatial_final", "training"), key=lambda k: kernel_ms[k] or 0.0)
     roof, roof_tc = None, None
-    if lpc is not None and kernel_ms["k_lp_generate"]:
+    if lpc is not None and kernel_ms["generate_stage"]:
         vox_bytes = 2
         per_px = lpc["generate_voxel_reads_px"] * vox_bytes + generate_stream_bytes_per_pixel(M_sel, lpc["vertices_px"], lpc["queries_px"])
         survey_px = lpc["generate_voxel_reads_px"] * vox_bytes + SURVEY_STREAM_PX
         alg = per_px * W * H
-        achieved = alg / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
-        achieved_s = survey_px * W * H / (kernel_ms["k_lp_generate"] / 1000.0) / 1e9
+        achieved = alg / (kernel_ms["generate_stage"] / 1000.0) / 1e9
+        achieved_s = survey_px * W * H / (kernel_ms["generate_stage"] / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": _traffic_from_profile("k_lp_generate"),
-                "kernel": "the generate stage (features, primary distance rounds, first vertices, and per bounce a sort, the walks and the vertices)",
+                "traffic": _traffic_from_profile("generate_stage"),
+                "kernel": "the generate stage (k_lp_rounds: features and primary distance rounds; k_lp_vertex0: first vertices; per bounce a sort, the walks and the vertices)",
                 "peak_source": peak_kind,
                 "dominant_by_time": dom, "algorithmic_bytes_per_launch": alg, "algorithmic_bytes_per_pixel": per_px,
                 "voxel_reads_per_pixel": lpc["generate_voxel_reads_px"], "vertex_records_per_pixel": lpc["vertices_px"],
-                "queries_per_pixel": lpc["queries_px"], "kernel_ms": kernel_ms["k_lp_generate"],
+                "queries_per_pixel": lpc["queries_px"], "kernel_ms": kernel_ms["generate_stage"],
                 "counts_from": f"oracle, learned form, frame 1 at {lpc['counted_at']}",
                 "stream_and_voxel_only": {"bytes_per_pixel": survey_px, "achieved": achieved_s, "frac": achieved_s / peak,
                                           "definition": "voxel reads x 2 B + the plain path's reservoir/feature stream bytes "
@@ -848,7 +848,7 @@ def main():
     ap.add_argument("--no-small", action="store_true", help="skip the 256^2 configurations (cfg1, cfg3, cfg4)")
     ap.add_argument("--no-animated", action="store_true", help="skip the animated-volume measurement")
     ap.add_argument("--batch-steps", type=int, default=4)
-    ap.add_argument("--batch-trials", type=int, default=6)
+    ap.add_argument("--batch-trials", type=int, default=9)
     ap.add_argument("--only-batched", action="store_true", help="run the batched form alone and print its summary")
     ap.add_argument("--no-batch-sequential", action="store_true", help="skip the batch's one-after-another comparison")
     args = ap.parse_args()

@@ -2074,9 +2074,13 @@ void noalloc_error(vr_context* c, const char* msg) { c->err = msg; }
 
 namespace vrk {
 #define VR_BDECL(MB)                                                                      \
-    void launch_batch_pass_##MB(const vrd::BatchLaunch&, int, int, cudaStream_t);       \
+    void launch_batch_pass_##MB(const vrd::BatchLaunch&, int, int, int, cudaStream_t);  \
     void launch_batch_train_gen_##MB(const vrd::BatchLaunch&, int, cudaStream_t);        \
-    void launch_batch_lp_bounce_##MB(const vrd::BatchLaunch&, int, int, int, int, cudaStream_t);
+    void launch_batch_lp_bounce_##MB(const vrd::BatchLaunch&, int, int, int, cudaStream_t); \
+    void launch_batch_split_march_##MB(const vrd::BatchLaunch&, int, cudaStream_t);      \
+    void launch_batch_split_reset_##MB(const vrd::BatchLaunch&, cudaStream_t);          \
+    void launch_batch_walk_all_##MB(const vrd::BatchLaunch&, int, int, cudaStream_t);     \
+    void launch_batch_vertex0_##MB(const vrd::BatchLaunch&, int, cudaStream_t);
 VR_BDECL(1) VR_BDECL(2) VR_BDECL(3) VR_BDECL(4)
 #undef VR_BDECL
 }  // namespace vrk
@@ -2096,12 +2100,16 @@ struct vr_batch {
     // the caller's stream by events (the legacy default stream cannot be captured)
     cudaStream_t gstream = nullptr;
     cudaEvent_t evIn = nullptr, evOut = nullptr;
+    // the training steps run on a stream of their own, forked after the select pass and joined
+    // at the end of the frame, concurrent with the spatial passes
+    cudaStream_t tstream = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     // graph
     bool useGraph = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<int64_t> sig;
-    int launches = 0;
+    int launches = 0, trainLaunches = 0;
     std::string err;
     // per-frame host state
     std::vector<CamFrame> cfs;
@@ -2118,18 +2126,47 @@ static void batch_drop_graph(vr_batch* b) {
 }
 
 template <int MB>
-static void batch_pass(const vrd::BatchLaunch& BL, int pass, int grid, cudaStream_t st) {
-    if (MB == 1) vrk::launch_batch_pass_1(BL, pass, grid, st);
-    else if (MB == 2) vrk::launch_batch_pass_2(BL, pass, grid, st);
-    else if (MB == 3) vrk::launch_batch_pass_3(BL, pass, grid, st);
-    else vrk::launch_batch_pass_4(BL, pass, grid, st);
+static void batch_pass(const vr_batch* b, const vrd::BatchLaunch& BL, int pass, cudaStream_t st) {
+    const int nsm = std::max(1, b->numSMs), bps = std::max(1, b->blocksPerSM);
+    if (MB == 1) vrk::launch_batch_pass_1(BL, pass, nsm, bps, st);
+    else if (MB == 2) vrk::launch_batch_pass_2(BL, pass, nsm, bps, st);
+    else if (MB == 3) vrk::launch_batch_pass_3(BL, pass, nsm, bps, st);
+    else vrk::launch_batch_pass_4(BL, pass, nsm, bps, st);
 }
 template <int MB>
-static void batch_lp_bounce(const vrd::BatchLaunch& BL, int inst, int bounce, int grid, int walk, cudaStream_t st) {
-    if (MB == 1) vrk::launch_batch_lp_bounce_1(BL, inst, bounce, grid, walk, st);
-    else if (MB == 2) vrk::launch_batch_lp_bounce_2(BL, inst, bounce, grid, walk, st);
-    else if (MB == 3) vrk::launch_batch_lp_bounce_3(BL, inst, bounce, grid, walk, st);
-    else vrk::launch_batch_lp_bounce_4(BL, inst, bounce, grid, walk, st);
+static void batch_lp_bounce(const vrd::BatchLaunch& BL, int inst, int bounce, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_lp_bounce_1(BL, inst, bounce, grid, st);
+    else if (MB == 2) vrk::launch_batch_lp_bounce_2(BL, inst, bounce, grid, st);
+    else if (MB == 3) vrk::launch_batch_lp_bounce_3(BL, inst, bounce, grid, st);
+    else vrk::launch_batch_lp_bounce_4(BL, inst, bounce, grid, st);
+}
+template <int MB>
+static void batch_split_march(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_split_march_1(BL, grid, st);
+    else if (MB == 2) vrk::launch_batch_split_march_2(BL, grid, st);
+    else if (MB == 3) vrk::launch_batch_split_march_3(BL, grid, st);
+    else vrk::launch_batch_split_march_4(BL, grid, st);
+}
+template <int MB>
+static void batch_walk_all(const vrd::BatchLaunch& BL, int bounce, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_walk_all_1(BL, bounce, grid, st);
+    else if (MB == 2) vrk::launch_batch_walk_all_2(BL, bounce, grid, st);
+    else if (MB == 3) vrk::launch_batch_walk_all_3(BL, bounce, grid, st);
+    else vrk::launch_batch_walk_all_4(BL, bounce, grid, st);
+}
+template <int MB>
+static void batch_vertex0(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_vertex0_1(BL, grid, st);
+    else if (MB == 2) vrk::launch_batch_vertex0_2(BL, grid, st);
+    else if (MB == 3) vrk::launch_batch_vertex0_3(BL, grid, st);
+    else vrk::launch_batch_vertex0_4(BL, grid, st);
+}
+template <int MB>
+static void batch_split_reset(const vrd::BatchLaunch& BL, cudaStream_t st) {
+    if (MB == 1) vrk::launch_batch_split_reset_1(BL, st);
+    else if (MB == 2) vrk::launch_batch_split_reset_2(BL, st);
+    else if (MB == 3) vrk::launch_batch_split_reset_3(BL, st);
+    else vrk::launch_batch_split_reset_4(BL, st);
 }
 template <int MB>
 static void batch_train_gen(const vrd::BatchLaunch& BL, int grid, cudaStream_t st) {
@@ -2186,7 +2223,7 @@ static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs,
     float* hCC = (float*)(b->hStage + instBytes + sceneBytes);
     const vrd::DevScene* dScene = (const vrd::DevScene*)(b->dData + instBytes);
     b->cfs.resize(n);
-    int tiles = 0, chunks = 0;
+    int tiles = 0, chunks = 0, cchunks = 0;
     sig.clear();
     sig.push_back(n); sig.push_back(b->tileW); sig.push_back(b->blocksPerSM); sig.push_back((int64_t)(size_t)b->dData);
     for (int i = 0; i < n; ++i) {
@@ -2205,12 +2242,16 @@ static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs,
         I.B.out = (float4*)outs[i];
         I.B.mvec = nullptr;
         I.learned = lp_active(c) ? 1 : 0;
+        I.walk = I.learned && !o.mInitialVisibilityUseLinearSampler ? 1 : 0;
         if (I.learned) {
             c->lp.targetMethod = o.mLearnedTargetMethod;
             I.L = c->lp;
             I.trainSeed = lp_train_seed(o.mLearnedSeed, c->frameCount);
         }
         I.spatialRounds = o.mEnableSpatialReuse ? o.mSpatialReuseRounds : 0;
+        // the split rounds where the single-instance frame takes them (the same result)
+        I.split = I.spatialRounds > 0 && c->split.seg && vrd::spatialSplitEligible(I.P) ? 1 : 0;
+        if (I.split) I.SS = c->split;
         int totalRoundId = 0;
         for (int r = 0; r < I.spatialRounds; ++r) {
             vrd::SpatialParams& S = I.S[r];
@@ -2232,12 +2273,14 @@ static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs,
         tiles += I.tilesX * ((c->H + b->tileH - 1) / b->tileH);
         I.trainChunkStart = chunks;
         if (I.learned && o.mLearnedTrainSamples > 0) chunks += (o.mLearnedTrainSamples + 127) / 128;
+        I.candChunkStart = cchunks;
+        if (I.learned) cchunks += (int)(((int64_t)o.mInitialM * c->W * c->H + 127) / 128);
         for (int k = 0; k < b->steps[i]; ++k) {
             const double t = (double)(c->adamStep + k + 1);
             hCC[b->ccOff[i] + 2 * k] = (float)(1.0 - std::pow(0.9, t));
             hCC[b->ccOff[i] + 2 * k + 1] = (float)(1.0 - std::pow(0.999, t));
         }
-        const int64_t s[] = {c->W, c->H, o.mInitialM, I.learned, I.spatialRounds, o.mLearnedTrainSamples, o.mLearnedBatch, b->steps[i],
+        const int64_t s[] = {c->W, c->H, o.mInitialM, I.learned, I.walk, I.spatialRounds, I.split, o.mLearnedTrainSamples, o.mLearnedBatch, b->steps[i],
                              (int64_t)(size_t)c->res[0].a, (int64_t)(size_t)c->lp.vrecA, (int64_t)(size_t)c->lp.train,
                              (int64_t)(size_t)c->netW, (int64_t)(size_t)c->netPart};
         sig.insert(sig.end(), s, s + sizeof(s) / sizeof(s[0]));
@@ -2249,6 +2292,7 @@ static int batch_prepare(vr_batch* b, const vr_camera* cams, float* const* outs,
     BL.tileH = b->tileH;
     BL.round = 0;
     BL.trainChunks = chunks;
+    BL.candChunks = cchunks;
     return VR_OK;
 }
 
@@ -2259,35 +2303,58 @@ static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
     cudaMemcpyAsync(b->dData, b->hStage, b->dataBytes, cudaMemcpyHostToDevice, st);
     const float* dCC = (const float*)(b->dData + instBytes + sceneBytes);
     const int grid = std::max(1, b->numSMs * b->blocksPerSM);
-    bool anyPlain = false, anyLearned = false, anyTrain = false;
-    for (vr_context* c : b->ctx) {
+    bool anyPlain = false, anyLearned = false, anyTrain = false, anySplit = false, anyUnsplit = false;
+    const vrd::BatchInstance* hInst = (const vrd::BatchInstance*)b->hStage;
+    for (int i = 0; i < n; ++i) {
+        vr_context* c = b->ctx[i];
         if (lp_active(c)) { anyLearned = true; anyTrain |= c->opts.mLearnedTrainSamples > 0; }
         else anyPlain = true;
+        if (hInst[i].spatialRounds > 0) (hInst[i].split ? anySplit : anyUnsplit) = true;
     }
     int launches = 0;
-    if (anyPlain) { batch_pass<MB>(BL, 0, grid, st); launches++; }
+    if (anyPlain) { batch_pass<MB>(b, BL, 0, st); launches++; }
     if (anyLearned) {
         for (vr_context* c : b->ctx)
             if (lp_active(c)) {
                 cudaMemsetAsync(c->lp.qcount, 0, sizeof(int), st);
                 cudaMemsetAsync(c->lp.pcount, 0, 16 * sizeof(int), st);
             }
-        batch_pass<MB>(BL, 1, grid, st);
-        launches++;
-        for (int i = 0; i < n; ++i)
-            if (lp_active(b->ctx[i]))
-                for (int bn = 1; bn < MB; ++bn) {
-                    const int walk = b->ctx[i]->opts.mInitialVisibilityUseLinearSampler ? 0 : 1;
-                    batch_lp_bounce<MB>(BL, i, bn, grid, walk, st);
-                    launches += 1 + walk;
-                }
+        batch_pass<MB>(b, BL, 1, st);
+        batch_vertex0<MB>(BL, grid, st);
+        launches += 2;
+        // the bounce passes: one launch each for the walks and the vertices of every walking
+        // instance, one per instance and bounce for the others (linear sampler)
+        bool anyWalk = false;
+        for (int i = 0; i < n; ++i) anyWalk |= hInst[i].walk != 0;
+        for (int bn = 1; bn < MB; ++bn) {
+            if (anyWalk) { batch_walk_all<MB>(BL, bn, grid, st); launches += 2; }
+            for (int i = 0; i < n; ++i)
+                if (hInst[i].learned && !hInst[i].walk) { batch_lp_bounce<MB>(BL, i, bn, grid, st); launches++; }
+        }
         for (vr_context* c : b->ctx)
             if (lp_active(c)) {
                 vrk::launch_net_infer(net_view(c), c->lp.query, c->lp.qcapacity, c->lp.qcount, c->lp.T, c->lp.qlist, c->status, c->numSMs, st);
                 launches++;
             }
-        batch_pass<MB>(BL, 2, grid, st);
+        batch_pass<MB>(b, BL, 2, st);
         launches++;
+        // online training of every learned instance on this frame's queries (used from the next
+        // frame on): training samples, then each instance's steps, on the training stream
+        if (anyTrain) {
+            cudaEventRecord(b->evFork, st);
+            cudaStreamWaitEvent(b->tstream, b->evFork, 0);
+            batch_train_gen<MB>(BL, grid, b->tstream);
+            b->trainLaunches = 1;
+            for (int i = 0; i < n; ++i) {
+                vr_context* c = b->ctx[i];
+                if (!lp_active(c) || c->opts.mLearnedTrainSamples <= 0) continue;
+                const int64_t step0 = c->adamStep;
+                lp_train_steps(c, c->lp.train, c->opts.mLearnedTrainSamples, b->tstream, dCC + b->ccOff[i]);
+                c->adamStep = step0;         // advanced once per frame in batch_finish (graph replays too)
+                b->trainLaunches += 2 * b->steps[i];
+            }
+            cudaEventRecord(b->evJoin, b->tstream);
+        }
     }
     if (b->temporal && !b->spatial) {
         for (vr_context* c : b->ctx) {
@@ -2300,24 +2367,28 @@ static void batch_launch(vr_batch* b, vrd::BatchLaunch BL, cudaStream_t st) {
     if (b->spatial) {
         for (int r = 0; r < b->rounds; ++r) {
             BL.round = r;
-            batch_pass<MB>(BL, 3, grid, st);
-            launches++;
+            if (anySplit) {
+                batch_split_reset<MB>(BL, st);
+                batch_pass<MB>(b, BL, 5, st);
+                batch_split_march<MB>(BL, grid, st);
+                batch_split_reset<MB>(BL, st);
+                batch_pass<MB>(b, BL, 6, st);
+                batch_split_march<MB>(BL, grid, st);
+                batch_pass<MB>(b, BL, 7, st);
+                launches += 7;
+            }
+            if (anyUnsplit) {
+                batch_pass<MB>(b, BL, 3, st);
+                launches++;
+            }
         }
     } else {
-        batch_pass<MB>(BL, 4, grid, st);
+        batch_pass<MB>(b, BL, 4, st);
         launches++;
     }
     if (anyTrain) {
-        batch_train_gen<MB>(BL, grid, st);
-        launches++;
-        for (int i = 0; i < n; ++i) {
-            vr_context* c = b->ctx[i];
-            if (!lp_active(c) || c->opts.mLearnedTrainSamples <= 0) continue;
-            const int64_t step0 = c->adamStep;
-            lp_train_steps(c, c->lp.train, c->opts.mLearnedTrainSamples, st, dCC + b->ccOff[i]);
-            c->adamStep = step0;         // advanced once per frame in batch_finish (graph replays too)
-            launches += 2 * b->steps[i];
-        }
+        cudaStreamWaitEvent(st, b->evJoin, 0);
+        launches += b->trainLaunches;
     }
     b->launches = launches;
 }
@@ -2413,6 +2484,9 @@ int vr_batch_create(vr_context* const* ctxs, int32_t n, vr_batch** out) {
     cudaEventCreateWithFlags(&b->evIn, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&b->evOut, cudaEventDisableTiming);
     cudaStreamCreateWithFlags(&b->gstream, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&b->tstream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&b->evJoin, cudaEventDisableTiming);
     *out = b;
     return VR_OK;
 }
@@ -2427,6 +2501,9 @@ void vr_batch_destroy(vr_batch* b) {
     if (b->evIn) cudaEventDestroy(b->evIn);
     if (b->evOut) cudaEventDestroy(b->evOut);
     if (b->gstream) cudaStreamDestroy(b->gstream);
+    if (b->evFork) cudaEventDestroy(b->evFork);
+    if (b->evJoin) cudaEventDestroy(b->evJoin);
+    if (b->tstream) cudaStreamDestroy(b->tstream);
     delete b;
 }
 
@@ -2462,7 +2539,8 @@ int32_t vr_batch_last_launch_count(const vr_batch* b) { return b ? b->launches :
 
 int vr_batch_autotune(vr_batch* b, const vr_camera* cams, float* const* outs, void* stream, float* trial_ms, int32_t max_trials) {
     if (!b || !cams || !outs) return VR_ERR_INVALID_ARG;
-    static const int shapes[][2] = {{8, 5}, {16, 5}, {32, 5}, {8, 3}, {16, 3}, {32, 3}, {8, 8}, {16, 8}, {32, 8}};
+    // tile widths x blocks per SM (capped per pass at the blocks it is compiled to keep resident)
+    static const int shapes[][2] = {{8, 5}, {16, 5}, {32, 5}, {8, 4}, {16, 4}, {32, 4}, {8, 3}, {16, 3}, {32, 3}};
     const int nShapes = (int)(sizeof(shapes) / sizeof(shapes[0]));
     cudaStream_t st = (cudaStream_t)stream;
     const bool graph = b->useGraph;

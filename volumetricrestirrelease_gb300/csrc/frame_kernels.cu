@@ -45,7 +45,9 @@ void VR_CAT(launch_reference_, VR_MB)(const vrd::FrameParams& P, int first, int 
 
 void VR_CAT(launch_lp_generate_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b,
                                         cudaStream_t st) {
-    vrd::k_lp_generate<VR_MB><<<g, b, 0, st>>>(P, B, L);
+    vrd::k_lp_rounds<VR_MB><<<g, b, 0, st>>>(P, B, L);
+    const size_t n = (size_t)P.initialM * (size_t)P.N;
+    vrd::k_lp_vertex0<VR_MB><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(P, L);
 }
 void VR_CAT(launch_lp_select_, VR_MB)(const vrd::FrameParams& P, const vrd::FrameBuffers& B, const vrd::LpBuffers& L, dim3 g, dim3 b,
                                       cudaStream_t st) {

@@ -616,10 +616,7 @@ __device__ __forceinline__ bool splitPixel(const FrameParams& P, int& px, int& p
 }
 
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_a(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
-                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
-    int px, py;
-    if (!splitPixel(P, px, py)) return;
+__device__ __forceinline__ void splitAPixel(const FrameParams& P, const FrameBuffers& B, const SpatialParams& S, const SpatialSplit& SS, int px, int py) {
     const int W = P.W, H = P.H, N = P.N, K = P.spatialK;
     const int pid = py * W + px;
     if (__ldg(&B.featCur[pid]) == 1.f) return;
@@ -647,10 +644,7 @@ __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_a(const __gr
 }
 
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_b(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
-                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
-    int px, py;
-    if (!splitPixel(P, px, py)) return;
+__device__ __forceinline__ void splitBPixel(const FrameParams& P, const FrameBuffers& B, const SpatialParams& S, const SpatialSplit& SS, int px, int py) {
     const int W = P.W, H = P.H, N = P.N, K = P.spatialK;
     const int pid = py * W + px;
     if (__ldg(&B.featCur[pid]) == 1.f) return;
@@ -688,8 +682,9 @@ __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_b(const __gr
     }
 }
 
-// the recorded segments, marched as resumable walks
-static __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_split_march(const __grid_constant__ SpatialSplit SS) {
+// the recorded segments of one list, marched as resumable walks by the warps of the grid: a lane
+// whose march ends takes the next listed segment; returns when the list is used up
+__device__ __forceinline__ void splitMarchList(const SpatialSplit& SS) {
     const int n = min(SS.counts[0], SS.capacity);
     const int lane = threadIdx.x & 31;
     MarchWalk w;
@@ -729,10 +724,7 @@ static __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_split_march
 }
 
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_c(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
-                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
-    int px, py;
-    if (!splitPixel(P, px, py)) return;
+__device__ __forceinline__ void splitCPixel(const FrameParams& P, const FrameBuffers& B, const SpatialParams& S, const SpatialSplit& SS, int px, int py) {
     const int W = P.W, H = P.H, N = P.N;
     const int pid = py * W + px;
     const ResBuf& in = B.sp[S.in];
@@ -810,6 +802,30 @@ __global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_c(const __gr
         finalShade<MB>(P, B, outb, result, px, py);
     }
 }
+
+#ifndef VR_BATCHED
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_a(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (splitPixel(P, px, py)) splitAPixel<MB>(P, B, S, SS, px, py);
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_b(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (splitPixel(P, px, py)) splitBPixel<MB>(P, B, S, SS, px, py);
+}
+static __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_split_march(const __grid_constant__ SpatialSplit SS) {
+    splitMarchList(SS);
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KSPAT_MIN_BLOCKS) k_split_c(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B,
+                                                                      const __grid_constant__ SpatialParams S, const __grid_constant__ SpatialSplit SS) {
+    int px, py;
+    if (splitPixel(P, px, py)) splitCPixel<MB>(P, B, S, SS, px, py);
+}
+#endif
 
 // k_final: FinalShading without spatial reuse (optionally after the history copy)
 template <int MB>

@@ -228,13 +228,13 @@ __device__ __forceinline__ void lpVertex0(const FrameParams& P, const LpBuffers&
 
 // generate, in the order of the learned target: GenerateFeatures, then per pixel the rounds of
 // TraceRays (up to 4 primary distance samples in one traversal) from the pixel's stream, whose
-// samples go to L.dist, then the first vertex of every candidate from the candidate's own stream
-// (the pixel's stream is left to the select pass).  With every round drawn before the first
-// vertex, the lanes of a warp walk their camera rays together and then build their vertices
-// together, instead of alternating between the two (same-box A/B at 1080p, 36 candidates: the
-// generate stage 72.7 -> 63.6 ms).
+// samples go to L.dist (the pixel's stream is then left to the select pass); then, in a launch of
+// its own with one thread per candidate, the first vertex of every candidate from the candidate's
+// own stream (lpVertex0).  Same-box A/B at 1080p, 36 candidates: the generate stage 72.7 ms with
+// rounds and vertices alternating per candidate, 63.5 ms with every round first in one kernel,
+// 55.8 ms with the vertices in their own launch (74 registers, a flat grid of M x N threads).
 template <int MB>
-__device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
+__device__ __forceinline__ void lpRoundsPixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
     const int W = P.W, N = P.N;
     const int pid = py * W + px;
     const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, P.H));
@@ -251,7 +251,6 @@ __device__ __forceinline__ void lpGeneratePixel(const FrameParams& P, const Fram
         for (int s = 0; s < rs; s++, c++) L.dist[(size_t)c * N + pid] = make_float4(hd[s], pd[s], trs[s], 0.f);
     }
     L.rng[pid] = make_uint4(sg.s[0], sg.s[1], sg.s[2], sg.s[3]);
-    for (c = 0; c < M; c++) lpVertex0<MB>(P, L, c, px, py);
 }
 
 // one indirect vertex (bounce b >= 1) of a queued path (entry i of `src`): its distance sample,
@@ -572,27 +571,32 @@ static __global__ void __launch_bounds__(256) k_path_scatter(const __grid_consta
         o[0] = a; o[1] = c; o[2] = d; o[3] = e;
     }
 }
+// generate in two launches: the per-pixel part (features and the rounds of primary distance
+// samples), then one thread per candidate for the first vertices (candidate c of pixel pid is
+// thread c * N + pid: the lanes of a warp take one candidate of neighbouring pixels)
 template <int MB>
-__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_generate(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_rounds(const __grid_constant__ FrameParams P, const __grid_constant__ FrameBuffers B, const __grid_constant__ LpBuffers L) {
     const int px = blockIdx.x * 8 + (threadIdx.x & 7);
     const int py = blockIdx.y * (blockDim.x >> 3) + (threadIdx.x >> 3);
     if (px >= P.W || py >= P.H) return;
-    lpGeneratePixel<MB>(P, B, L, px, py);
+    lpRoundsPixel<MB>(P, B, L, px, py);
+}
+template <int MB>
+__global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex0(const __grid_constant__ FrameParams P, const __grid_constant__ LpBuffers L) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (size_t)P.initialM * (size_t)P.N) return;
+    const int c = (int)(i / (size_t)P.N), pid = (int)(i - (size_t)c * (size_t)P.N);
+    lpVertex0<MB>(P, L, c, pid % P.W, pid / P.W);
 }
 
 // select: resample the recorded candidates with the predicted transmittance, then finish
-// TraceRays (p_hat of the winner) and run TemporalReuse as k_initial does
+// TraceRays (p_hat of the winner) and run TemporalReuse as k_initial does.
+// lpSelectChoose: the candidates of a pixel resampled with the predicted transmittances (the
+// recorded vertices replayed with p-hat = unoccluded p-hat x T); the winner's suffix goes to
+// B.cur.extra
 template <int MB>
-__device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
-    const int W = P.W, N = P.N;
-    const int pid = py * W + px;
-    const f3 dir = vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, W, P.H));
-    const Ray ray{P.camPos, dir, 0.f, kRayTMax};
-    vr::Rng sg;
-    {
-        uint4 s = L.rng[pid];
-        sg.s[0] = s.x; sg.s[1] = s.y; sg.s[2] = s.z; sg.s[3] = s.w;
-    }
+__device__ __forceinline__ Reservoir lpSelectChoose(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int pid) {
+    const int N = P.N;
     f3 finalEx[4] = {mk3(0.f), mk3(0.f), mk3(0.f), mk3(0.f)};
     Reservoir fin = newReservoir();
     for (int c = 0; c < P.initialM; c++) {
@@ -628,14 +632,33 @@ __device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameB
     const int mib0 = decodeBounces(fin.sampledPixel, MB);
     for (int b = 0; b < mib0; b++) B.cur.extra[(size_t)b * N + pid] = make_float4(finalEx[b].x, finalEx[b].y, finalEx[b].z, 0.f);
     fin.startPixel = pid;
-    float ph = evalPHat(fin, B.cur.extra, N, ray, sg, P.spatial, MB);
+    return fin;
+}
+// TraceRays' p-hat of the winner (the marched target) in place of the predicted one
+__device__ __forceinline__ void lpSelectTarget(Reservoir& fin, float ph) {
     if (fin.runningSum > 0.f) {
         fin.runningSum *= fin.p_y == 0.f ? 0.f : ph / fin.p_y;
         fin.p_y = ph;
     }
+}
+__device__ __forceinline__ vr::Rng lpPixelStream(const LpBuffers& L, int pid) {
+    vr::Rng sg;
+    const uint4 s = L.rng[pid];
+    sg.s[0] = s.x; sg.s[1] = s.y; sg.s[2] = s.z; sg.s[3] = s.w;
+    return sg;
+}
+
+template <int MB>
+__device__ __forceinline__ void lpSelectPixel(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int px, int py) {
+    const int pid = py * P.W + px;
+    const Ray ray{P.camPos, vr::normalize(pinholeDir(P.camU, P.camV, P.camW, px, py, P.W, P.H)), 0.f, kRayTMax};
+    vr::Rng sg = lpPixelStream(L, pid);
+    Reservoir fin = lpSelectChoose<MB>(P, B, L, pid);
+    lpSelectTarget(fin, evalPHat(fin, B.cur.extra, P.N, ray, sg, P.spatial, MB));
     storeRes(B.cur, pid, fin);
     if (P.temporalEnabled && !P.isFirstFrame) temporalReuse<MB>(P, B, px, py, ray);
 }
+
 // 4 blocks per SM (128 registers): the spills of the temporal evaluations drop from 188 to 88
 // bytes; measured 14.2 -> 13.7 ms per 1080p frame (3 blocks: 14.95 ms)
 template <int MB>
