@@ -597,40 +597,53 @@ __global__ void __launch_bounds__(128, VR_KINIT_MIN_BLOCKS) k_lp_vertex0(const _
 template <int MB>
 __device__ __forceinline__ Reservoir lpSelectChoose(const FrameParams& P, const FrameBuffers& B, const LpBuffers& L, int pid) {
     const int N = P.N;
-    f3 finalEx[4] = {mk3(0.f), mk3(0.f), mk3(0.f), mk3(0.f)};
     Reservoir fin = newReservoir();
+    int cSel = -1;
     for (int c = 0; c < P.initialM; c++) {
+        // a candidate's records are loaded before they are replayed, so that their loads are in
+        // flight together: every vertex record's flags, then the record and T of each vertex up
+        // to the first invalid one (the slots after it are never used)
         const float2 cr = L.crec[(size_t)c * N + pid];
-        Reservoir comb = newReservoir();
+        int4 rb[MB];
+#pragma unroll
+        for (int b = 0; b < MB; b++) rb[b] = L.vrecB[(size_t)(c * MB + b) * N + pid];
+        float4 ra[MB];
+        float tv[MB];
+        bool alive = true;
+#pragma unroll
         for (int b = 0; b < MB; b++) {
             const size_t slot = (size_t)(c * MB + b) * N + pid;
-            const int4 rb = L.vrecB[slot];
-            if (!(rb.z & kLpValid)) break;
-            const float4 ra = L.vrecA[slot];
+            alive = alive && (rb[b].z & kLpValid);
+            ra[b] = alive ? L.vrecA[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+            tv[b] = alive && (rb[b].z & kLpNeedsT) ? L.T[slot] : 1.f;
+        }
+        Reservoir comb = newReservoir();
+#pragma unroll
+        for (int b = 0; b < MB; b++) {
+            if (!(rb[b].z & kLpValid)) break;
             Reservoir out = newReservoir();
             out.M = 1; out.depth = cr.x;
-            out.runningSum = ra.x; out.p_y = ra.y; out.uv0 = ra.z; out.uv1 = ra.w;
-            out.lightID = rb.x; out.sampledPixel = rb.y;
-            if (rb.z & kLpNeedsT) {
-                float p_y = ra.y * L.T[slot];
-                out.runningSum = ra.x == 0.f ? 0.f : p_y / ra.x;
+            out.runningSum = ra[b].x; out.p_y = ra[b].y; out.uv0 = ra[b].z; out.uv1 = ra[b].w;
+            out.lightID = rb[b].x; out.sampledPixel = rb[b].y;
+            if (rb[b].z & kLpNeedsT) {
+                float p_y = ra[b].y * tv[b];
+                out.runningSum = ra[b].x == 0.f ? 0.f : p_y / ra[b].x;
                 out.p_y = p_y;
             }
-            if (MB > 1) resampleStepU(out, comb, __int_as_float(rb.w));
+            if (MB > 1) resampleStepU(out, comb, __int_as_float(rb[b].w));
             else comb = out;
         }
         if (MB > 1) comb.M = 1;
-        bool sel = resampleStepU(comb, fin, cr.y);
-        if (sel && MB > 1) {
-            int mib = decodeBounces(fin.sampledPixel, MB);
-            for (int b = 0; b < mib; b++) {
-                float4 e = L.ex[(size_t)(c * (MB - 1) + b) * N + pid];
-                finalEx[b] = mk3(e.x, e.y, e.z);
-            }
+        if (resampleStepU(comb, fin, cr.y)) cSel = c;
+    }
+    // the winner's suffix (its candidate's records are not written again in the frame)
+    if (MB > 1 && cSel >= 0) {
+        const int mib0 = decodeBounces(fin.sampledPixel, MB);
+        for (int b = 0; b < mib0; b++) {
+            const float4 e = L.ex[(size_t)(cSel * (MB - 1) + b) * N + pid];
+            B.cur.extra[(size_t)b * N + pid] = make_float4(e.x, e.y, e.z, 0.f);
         }
     }
-    const int mib0 = decodeBounces(fin.sampledPixel, MB);
-    for (int b = 0; b < mib0; b++) B.cur.extra[(size_t)b * N + pid] = make_float4(finalEx[b].x, finalEx[b].y, finalEx[b].z, 0.f);
     fin.startPixel = pid;
     return fin;
 }
