@@ -756,6 +756,11 @@ struct CellByDensity {
     __device__ void end() {}
 };
 
+// The largest float x with vr::exp_(x) < 0.01f (bits 0xc0935d8f): exp_ is non-decreasing, so
+// "exp_(Tr) < 0.01f", the early exit of the feature march, is "Tr <= kFeatureCutoff", without an
+// exponential per step (tests/test_feature_cutoff.py checks the equivalence over every float of
+// [-5.3, -4.4] and on samples of the rest).
+constexpr float kFeatureCutoff = -4.60517073f;
 struct FeatureMarch {
     float accu = 1.f; float tNear, tFar; Ray ray; float Tr = 0.f; bool lin; float tStep; bool init = false;
     __device__ void setRay(float a, float b, const Ray& r) { tNear = a; tFar = b; ray = r; }
@@ -766,14 +771,28 @@ struct FeatureMarch {
         f3 wp = ray.o + t * ray.d;
         f3 p = wp - vl;
         const f3 wpt = tStep * ray.d;
-        for (int iter = 0; iter < kMaxBrickSteps && inLeafF(p); iter++) {
-            float cur = vr::exp_(Tr);
-            if (cur < 0.01f) { end(); return true; }
-            float sigma_t = densityLocal(mip, brick, p, lin) * c_scene.sigma_t;
-            float neg = -sigma_t * tStep;
-            Tr += neg;
+        // two samples per trip, as in TrRayMarch: the second sample's density is loaded with the
+        // first (a read inside the brick, used only if the march gets there), and the steps are
+        // taken one by one with the early exit tested before each, as in the one-sample loop
+        int iter = 0;
+        while (iter < kMaxBrickSteps && inLeafF(p)) {
+            const f3 p1 = p + wpt;
+            const bool second = iter + 1 < kMaxBrickSteps && inLeafF(p1);
+            const float d0 = densityLocal(mip, brick, p, lin);
+            const float d1 = second ? densityLocal(mip, brick, p1, lin) : 0.f;
+            if (Tr <= kFeatureCutoff) { end(); return true; }
+            float sigma_t = d0 * c_scene.sigma_t;
+            Tr += -sigma_t * tStep;
+            p = p1;
+            t += tStep;
+            iter++;
+            if (!second) continue;
+            if (Tr <= kFeatureCutoff) { end(); return true; }
+            sigma_t = d1 * c_scene.sigma_t;
+            Tr += -sigma_t * tStep;
             p = p + wpt;
             t += tStep;
+            iter++;
         }
         return false;
     }
