@@ -230,7 +230,7 @@ __device__ __forceinline__ void lpVertex0(const FrameParams& P, const LpBuffers&
 // TraceRays (up to 4 primary distance samples in one traversal) from the pixel's stream, whose
 // samples go to L.dist (the pixel's stream is then left to the select pass); then, in a launch of
 // its own with one thread per candidate, the first vertex of every candidate from the candidate's
-// own stream (lpVertex0).  Same-box A/B at 1080p, 36 candidates: the generate stage 72.7 ms with
+// own stream (lpVertex0).  Measured on one GB300 at 1080p, 36 candidates: the generate stage 72.7 ms with
 // rounds and vertices alternating per candidate, 63.5 ms with every round first in one kernel,
 // 55.8 ms with the vertices in their own launch (74 registers, a flat grid of M x N threads).
 template <int MB>
