@@ -599,14 +599,24 @@ __device__ __forceinline__ Reservoir lpSelectChoose(const FrameParams& P, const 
     const int N = P.N;
     Reservoir fin = newReservoir();
     int cSel = -1;
+    // a candidate's records are loaded before they are replayed, so that their loads are in
+    // flight together: every vertex record's flags (fetched while the previous candidate is
+    // replayed), then the record and T of each vertex up to the first invalid one (the slots
+    // after it are never used)
+    float2 crNext = L.crec[pid];
+    int4 rbNext[MB];
+#pragma unroll
+    for (int b = 0; b < MB; b++) rbNext[b] = L.vrecB[(size_t)b * N + pid];
     for (int c = 0; c < P.initialM; c++) {
-        // a candidate's records are loaded before they are replayed, so that their loads are in
-        // flight together: every vertex record's flags, then the record and T of each vertex up
-        // to the first invalid one (the slots after it are never used)
-        const float2 cr = L.crec[(size_t)c * N + pid];
+        const float2 cr = crNext;
         int4 rb[MB];
 #pragma unroll
-        for (int b = 0; b < MB; b++) rb[b] = L.vrecB[(size_t)(c * MB + b) * N + pid];
+        for (int b = 0; b < MB; b++) rb[b] = rbNext[b];
+        if (c + 1 < P.initialM) {
+            crNext = L.crec[(size_t)(c + 1) * N + pid];
+#pragma unroll
+            for (int b = 0; b < MB; b++) rbNext[b] = L.vrecB[(size_t)((c + 1) * MB + b) * N + pid];
+        }
         float4 ra[MB];
         float tv[MB];
         bool alive = true;
